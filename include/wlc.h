@@ -1,0 +1,149 @@
+/*
+ * wlc.h -- C ABI of the GB300 (sm_103a) wormlike-chain MDE hot path.
+ *
+ * Drop-in boundary for the propagator / density entry points of
+ * tjz2026/wormlike-chain-triblock.  The reference keeps all state in Fortran
+ * module globals (global_parameters.f90:17-376) and has no bind(C) interface;
+ * each entry point below replaces one reference routine (file:line cited) and
+ * keeps that routine's meaning.  A Fortran host binds these through
+ * ISO_C_BINDING.
+ *
+ * Conventions
+ *  - Every function returns 0 on success or a negative WLC_E_* code;
+ *    wlc_last_error() gives a message.  No call aborts the process and no
+ *    call falls back to a CPU path.
+ *  - Host arrays are plain pointers with the reference's Fortran
+ *    (column-major) layouts, written here as C index expressions.  Grid
+ *    point r = x + nx*(y + ny*z) (the reference's x-pencil index on one
+ *    rank, grid_mod.f90:356-379).  The library copies in and out; it never
+ *    keeps a host pointer.
+ *  - A context owns one CUDA stream and all device memory of one SCFT
+ *    instance; it is not thread-safe.  One context per host thread.
+ */
+#ifndef WLC_H
+#define WLC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define WLC_ABI_VERSION 1
+
+enum {
+    WLC_OK = 0,
+    WLC_E_PARAM = -1,     /* invalid parameter (odd block length, bad size ...) */
+    WLC_E_ALLOC = -2,     /* device or host allocation failed                   */
+    WLC_E_CUDA = -3,      /* CUDA runtime error                                 */
+    WLC_E_STATE = -4,     /* call order violated (e.g. density before sweeps)   */
+    WLC_E_NONFINITE = -5, /* NaN/Inf detected in a result                       */
+    WLC_E_UNSUPPORTED = -6, /* size/option combination not built                */
+    WLC_E_SELFTEST = -7   /* host-side consistency check of the G(k) factorisation failed */
+};
+
+enum { WLC_FP64 = 0, WLC_FP32 = 1 };
+
+/* Fortran literal semantics of the reference's default-kind constants
+ * (11.0/6.0, 1.0/3.0, 1.0/sqrt(3.0), sqrt(1.0*...) in triple_product, PI of
+ * kind SP): WLC_LIT_REAL4 = standard build (single precision),
+ * WLC_LIT_REAL8 = build with a default-real-8 promotion flag. */
+enum { WLC_LIT_REAL4 = 0, WLC_LIT_REAL8 = 1 };
+
+/* Parameters of one ABC triblock instance: the union of input.txt
+ * (initialize_mod.f90:59-84) and the reference's compile-time constants
+ * (global_parameters.f90:32,52-60), with one L for all blocks. */
+typedef struct wlc_params {
+    int32_t n[3];       /* SIDEx, SIDEy, SIDEz (even)                              */
+    int32_t lmax;       /* L: harmonics l = 0..L, M = (L+1)^2 coefficients          */
+    int32_t nmax;       /* Nmax contour steps, ds = 1/Nmax                          */
+    int32_t ns[3];      /* NA, NB, NC (even, NA+NB+NC = Nmax, initialize_mod.f90:190) */
+    double dx[3];       /* grid spacing dx, dy, dz (box edge / SIDE)                */
+    double loa;         /* Loa (L over a)                                           */
+    double kappa[3];    /* kapa_A (0.5 in the reference), kapa_B, kapa_C            */
+    double chi[3];      /* NxAB, NxAC, NxBC                                         */
+    double nmu;         /* Maier-Saupe NMu (0 disables the Theta term)              */
+    int32_t precision;  /* WLC_FP64 (drop-in) or WLC_FP32 propagators               */
+    int32_t literals;   /* WLC_LIT_REAL4 or WLC_LIT_REAL8                            */
+    int32_t store_qstar;/* 1: keep every q* slice (wlc_get_q on dir -1 works)       */
+    int32_t reserved[5];
+} wlc_params;
+
+typedef struct wlc_ctx wlc_ctx;
+
+/* ABI version of the loaded library (WLC_ABI_VERSION). */
+int wlc_abi_version(void);
+
+/* Allocate an instance on the current CUDA device, build the harmonic
+ * algebra (init_arrays_2decomp, init_array_2dcomp_mod.f90:7-375) and the
+ * k-space operator data (init_inverse_sparse_GAB,
+ * Gmatrix_2dcomp_mod.f90:222-652). */
+int wlc_create(const wlc_params* p, wlc_ctx** out);
+int wlc_destroy(wlc_ctx* ctx);
+const char* wlc_last_error(const wlc_ctx* ctx);
+
+/* Change the grid spacing and rebuild the k-space data; the reference calls
+ * init_inverse_sparse_GAB every time the box changes
+ * (Gmatrix_2dcomp_mod.f90:222-224, SCFT_control.f90:166-183). */
+int wlc_set_box(wlc_ctx* ctx, double dx, double dy, double dz);
+
+/* Upload the block fields W_blk(0:LS,1:3) (w[blk*nr + r]) and, when
+ * nmu != 0, M_OP(0:LS,0:2,0:2) (m_op[r + nr*(a + 3*b)]; may be NULL).
+ * Replaces the module-global assignment the Fortran host does before
+ * calc_THETAij / MDE_q (SCFT_control.f90:237-243). */
+int wlc_set_fields(wlc_ctx* ctx, const double* w, const double* m_op);
+
+/* Forward (dir=+1, MDE_q, wormlike_MDE_2dcomp_mod.f90:231-959) or backward
+ * (dir=-1, MDE_qstar, :961-1557) propagator sweep over the three blocks, as
+ * ABC_melt_driver (MDE_ABC.f90:8-88) orders them. */
+int wlc_propagate(wlc_ctx* ctx, int32_t dir);
+
+/* density() (SCFT_Density_FE_ABC.f90:3-271, per-block restatement).
+ * phi:  R_blk(0:LS,1:3)            -> phi[blk*nr + r]            (may be NULL)
+ * junc: junction densities at s = NA, NA+NB, Nmax -> junc[j*nr + r] (may be NULL)
+ * s_op: S_OP_blk(0:LS,0:2,0:2,1:3) -> s_op[r + nr*(a + 3*b + 9*blk)] (may be NULL;
+ *       computing it costs ~ nnz(J)*Nmax*nr flops)
+ * lnq:  pff_global = ln Q            (may be NULL) */
+int wlc_density(wlc_ctx* ctx, double* phi, double* junc, double* s_op, double* lnq);
+
+/* free_energy() (SCFT_Density_FE.f90:273-342, three-block form): uses the
+ * last wlc_density result and the current fields. */
+int wlc_free_energy(wlc_ctx* ctx, double* fe);
+
+/* Copy one contour slice q_f(0:M-1,0:LS,s) (dir=+1) or q_star(...,s)
+ * (dir=-1) to the host: out[r*M + i] (coefficient fastest, as the
+ * reference's q_f(i,K,s)). */
+int wlc_get_q(wlc_ctx* ctx, int32_t dir, int32_t s, double* out);
+
+/* Overwrite one contour slice (test hook; same layout as wlc_get_q). */
+int wlc_set_q(wlc_ctx* ctx, int32_t dir, int32_t s, const double* in);
+
+/* init_pr(s, blk_indx, dir, M_Bar, Pr) (MDE_ABC.f90:223-383): BDF right-hand
+ * side of contour index s from the stored slices; pr[r*M + i]. */
+int wlc_init_pr(wlc_ctx* ctx, int32_t dir, int32_t s, double* pr);
+
+/* mde_one_step(M_Bar, q_out, Pr, G_index, blk_indx, dir) (MDE_ABC.f90:90-221):
+ * q_out = C2R(G^-1 . R2C(Pr))/N^3 for the ABC G_index table of
+ * Gmatrix_mod-old.f90:446-518 (1 GA1, 2 GA2, 3 GA3, 4 GB3, 5 GC3, 6 GA3*,
+ * 7 GB3*, 8 GC3*, 9 GC2*, 10 GC1*).  pr, q_out: [r*M + i] host arrays. */
+int wlc_mde_one_step(wlc_ctx* ctx, int32_t g_index, const double* pr, double* q_out);
+
+/* Number of the library's own kernel launches issued on the context's
+ * stream since creation (instrumentation). */
+int64_t wlc_launch_count(const wlc_ctx* ctx);
+
+/* The CUDA stream the context launches on (cudaStream_t as void*), for
+ * event timing by the caller. */
+void* wlc_stream(const wlc_ctx* ctx);
+
+/* Device time (ms, CUDA events on the context stream) of the last
+ * wlc_propagate, split by kernel family: [0] rhs+xy-FFT, [1] z-FFT+G solve,
+ * [2] inverse xy-FFT, [3] total.  Only filled when timing is enabled
+ * (wlc_enable_timing). */
+int wlc_enable_timing(wlc_ctx* ctx, int32_t on);
+int wlc_last_timing(const wlc_ctx* ctx, double* ms4);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* WLC_H */

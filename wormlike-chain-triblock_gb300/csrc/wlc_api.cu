@@ -1,0 +1,765 @@
+// wlc_api.cu -- the C ABI (include/wlc.h): one context per SCFT instance,
+// owning its CUDA stream and device memory.  Sweep drivers follow
+// ABC_melt_driver (MDE_ABC.f90:8-88); density / free energy follow
+// SCFT_Density_FE_ABC.f90:3-271 and SCFT_Density_FE.f90:273-342.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "wlc.h"
+#include "wlc_internal.h"
+#include "wlc_reduce.h"
+#include "wlc_step.h"
+
+using namespace wlc;
+
+struct wlc_ctx {
+    wlc_params p{};
+    int N = 0, L = 0, M = 0, nkx = 0;
+    int64_t nr = 0, nk = 0;
+    bool fp32 = false;
+    int real4 = 1;
+    double ds = 0, vol = 0, kf[3] = {0, 0, 0};
+    int nstart[3] = {0, 0, 0};
+    int kc = 1;
+    cudaStream_t st = nullptr;
+    std::string err;
+    BasisTables tab;
+    std::vector<void*> allocs;
+    SolveTablesT<double> sd{};
+    SolveTablesT<float> sf{};
+    ThetaLists thl{};
+    JLists jl{};
+    void* twg = nullptr;
+    void* qf = nullptr;
+    void* qb = nullptr;
+    void* phat = nullptr;
+    void* cf = nullptr;
+    void* work = nullptr;    // [M][nr] compute type: RHS / one-step scratch
+    void* msterm = nullptr;  // [M][nr] compute type: Maier-Saupe term
+    double* w = nullptr;
+    double* mop = nullptr;
+    double* raw = nullptr;   // [3][nr]
+    double* junc = nullptr;  // [3][nr]
+    double* qend = nullptr;  // [nr]
+    double* phi = nullptr;   // [3][nr]
+    double* part = nullptr;  // [kS3Blocks]
+    double* scal = nullptr;  // [8]
+    double* sraw = nullptr;  // [3][5][nr]
+    double* ar = nullptr;    // [nr]
+    double* stage = nullptr; // [M*nr] double, host transfer staging
+    int* flag = nullptr;
+    bool have_fields = false, have_mop = false, have_fwd = false, have_bwd = false, have_density = false;
+    double lnq = 0.0, totden = 0.0;
+    int64_t launches = 0;
+    bool timing = false;
+    std::vector<cudaEvent_t> ev;
+    double tms[4] = {0, 0, 0, 0};
+};
+
+static int set_err(wlc_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+#define CK(call)                                                                                          \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return set_err(c, WLC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
+    } while (0)
+
+template <typename X> static int dalloc(wlc_ctx* c, X** ptr, size_t bytes) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        char buf[200];
+        std::snprintf(buf, sizeof buf, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+        return set_err(c, WLC_E_ALLOC, buf);
+    }
+    c->allocs.push_back(p);
+    *ptr = reinterpret_cast<X*>(p);
+    return WLC_OK;
+}
+
+template <typename X> static int upload(wlc_ctx* c, X** dst, const std::vector<X>& v) {
+    int rc = dalloc(c, dst, sizeof(X) * v.size());
+    if (rc) return rc;
+    if (!v.empty()) CK(cudaMemcpy((void*)*dst, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice));
+    return WLC_OK;
+}
+
+template <typename T> static int build_solve_tables(wlc_ctx* c, SolveTablesT<T>& s) {
+    const BasisTables& t = c->tab;
+    s.L = t.L;
+    s.M = t.M;
+    std::vector<int16_t> pairs;
+    for (int l = 1; l <= t.L; ++l)
+        for (int m = 1; m <= l; ++m) {
+            pairs.push_back((int16_t)(l * l + l + m));
+            pairs.push_back((int16_t)(l * l + l - m));
+            pairs.push_back((int16_t)m);
+        }
+    s.npairs = (int)pairs.size() / 3;
+    auto cvt = [](const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); };
+    auto i16 = [](const std::vector<int>& v) {
+        std::vector<int16_t> o(v.size());
+        for (size_t k = 0; k < v.size(); ++k) o[k] = (int16_t)v[k];
+        return o;
+    };
+    int rc;
+    int16_t* p16;
+    int* pi;
+    T* pv;
+    if ((rc = upload(c, &p16, pairs))) return rc;
+    s.pairs = p16;
+    if ((rc = upload(c, &pi, t.xp_ptr))) return rc;
+    s.xp_ptr = pi;
+    if ((rc = upload(c, &p16, i16(t.xp_col)))) return rc;
+    s.xp_col = p16;
+    if ((rc = upload(c, &pv, cvt(t.xp_val)))) return rc;
+    s.xp_val = pv;
+    if ((rc = upload(c, &pi, t.xm_ptr))) return rc;
+    s.xm_ptr = pi;
+    if ((rc = upload(c, &p16, i16(t.xm_col)))) return rc;
+    s.xm_col = p16;
+    if ((rc = upload(c, &pv, cvt(t.xm_val)))) return rc;
+    s.xm_val = pv;
+    if ((rc = upload(c, &pv, cvt(t.zoff)))) return rc;
+    s.zoff = pv;
+    // correction entries, CSR over rows
+    std::vector<std::vector<std::pair<int, std::pair<int, double>>>> rows(t.M);
+    for (int a = 0; a < 3; ++a)
+        for (size_t e = 0; e < t.dR[a].size(); ++e)
+            rows[t.dR[a].row[e]].push_back({t.dR[a].col[e], {a, t.dR[a].val[e]}});
+    std::vector<int> ptr(t.M + 1, 0);
+    std::vector<int16_t> col;
+    std::vector<int8_t> axis;
+    std::vector<T> val;
+    for (int i = 0; i < t.M; ++i) {
+        for (auto& e : rows[i]) {
+            col.push_back((int16_t)e.first);
+            axis.push_back((int8_t)e.second.first);
+            val.push_back((T)e.second.second);
+        }
+        ptr[i + 1] = (int)val.size();
+    }
+    s.ndr = (int)val.size();
+    int8_t* p8;
+    if ((rc = upload(c, &pi, ptr))) return rc;
+    s.dr_ptr = pi;
+    if ((rc = upload(c, &p16, col))) return rc;
+    s.dr_col = p16;
+    if ((rc = upload(c, &p8, axis))) return rc;
+    s.dr_axis = p8;
+    if ((rc = upload(c, &pv, val))) return rc;
+    s.dr_val = pv;
+    return WLC_OK;
+}
+
+template <typename T> static int build_twiddles(wlc_ctx* c) {
+    using C = typename cvec<T>::t;
+    std::vector<C> tw(c->N);
+    for (int j = 0; j < c->N; ++j) {
+        const double a = 2.0 * M_PI * (double)j / (double)c->N;
+        tw[j].x = (T)std::cos(a);
+        tw[j].y = (T)(-std::sin(a));
+    }
+    C* d;
+    int rc = upload(c, &d, tw);
+    c->twg = d;
+    return rc;
+}
+
+extern "C" int wlc_abi_version(void) { return WLC_ABI_VERSION; }
+
+extern "C" const char* wlc_last_error(const wlc_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+extern "C" int64_t wlc_launch_count(const wlc_ctx* c) { return c ? c->launches : 0; }
+
+extern "C" void* wlc_stream(const wlc_ctx* c) { return c ? (void*)c->st : nullptr; }
+
+static int validate(const wlc_params* p, std::string& why) {
+    char buf[256];
+    if (p->n[0] != p->n[1] || p->n[1] != p->n[2]) {
+        why = "only cubic grids (SIDEx = SIDEy = SIDEz) are built";
+        return WLC_E_UNSUPPORTED;
+    }
+    if (!supported_n(p->n[0])) {
+        std::snprintf(buf, sizeof buf, "grid edge %d has no compiled kernels", p->n[0]);
+        why = buf;
+        return WLC_E_UNSUPPORTED;
+    }
+    if (p->lmax < 0 || p->lmax > 15) {
+        why = "lmax must be in [0, 15]";
+        return WLC_E_PARAM;
+    }
+    if (p->nmax < 3) {
+        why = "nmax must be >= 3";
+        return WLC_E_PARAM;
+    }
+    int sum = 0;
+    for (int b = 0; b < 3; ++b) {
+        if (p->ns[b] < 0 || (p->ns[b] % 2) != 0) {
+            std::snprintf(buf, sizeof buf, "block lengths must be even and >= 0 (NA,NB,NC = %d,%d,%d)", p->ns[0],
+                          p->ns[1], p->ns[2]);
+            why = buf;
+            return WLC_E_PARAM;
+        }
+        sum += p->ns[b];
+        if (!(p->kappa[b] > 0)) {
+            why = "kappa must be > 0";
+            return WLC_E_PARAM;
+        }
+        if (!(p->dx[b] > 0)) {
+            why = "grid spacing must be > 0";
+            return WLC_E_PARAM;
+        }
+    }
+    if (sum != p->nmax) {
+        why = "NA + NB + NC must equal nmax";
+        return WLC_E_PARAM;
+    }
+    if (p->precision != WLC_FP64 && p->precision != WLC_FP32) {
+        why = "precision must be WLC_FP64 or WLC_FP32";
+        return WLC_E_PARAM;
+    }
+    if (p->literals != WLC_LIT_REAL4 && p->literals != WLC_LIT_REAL8) {
+        why = "literals must be WLC_LIT_REAL4 or WLC_LIT_REAL8";
+        return WLC_E_PARAM;
+    }
+    return WLC_OK;
+}
+
+static void apply_box(wlc_ctx* c) {
+    for (int a = 0; a < 3; ++a) c->kf[a] = lit_kfactor(c->N, c->p.dx[a], c->real4);
+    c->vol = c->p.dx[0] * c->p.dx[1] * c->p.dx[2] * (double)c->nr;  // SCFT_control.f90:180
+}
+
+template <typename T> static int alloc_fields(wlc_ctx* c) {
+    using C = typename cvec<T>::t;
+    const size_t sl = (size_t)c->M * c->nr;
+    int rc;
+    T* pt;
+    C* pc;
+    if ((rc = dalloc(c, &pt, sizeof(T) * sl * (c->p.nmax + 1)))) return rc;
+    c->qf = pt;
+    if ((rc = dalloc(c, &pt, sizeof(T) * sl * (c->p.nmax + 1)))) return rc;
+    c->qb = pt;
+    if ((rc = dalloc(c, &pc, sizeof(C) * (size_t)c->nk * c->M))) return rc;
+    c->phat = pc;
+    if ((rc = dalloc(c, &pt, sizeof(T) * 9 * (size_t)c->nr))) return rc;
+    c->cf = pt;
+    if ((rc = dalloc(c, &pt, sizeof(T) * sl))) return rc;
+    c->work = pt;
+    if (std::fabs(c->p.nmu) >= 1.0e-5) {
+        if ((rc = dalloc(c, &pt, sizeof(T) * sl))) return rc;
+        c->msterm = pt;
+    }
+    return build_twiddles<T>(c);
+}
+
+extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
+    if (!p || !out) return WLC_E_PARAM;
+    *out = nullptr;
+    wlc_ctx* c = new wlc_ctx();
+    std::string why;
+    int rc = validate(p, why);
+    if (rc) {
+        // the caller gets the code; keep the message reachable through a
+        // context that only carries the error
+        c->err = why;
+        *out = c;
+        return rc;
+    }
+    c->p = *p;
+    c->N = p->n[0];
+    c->L = p->lmax;
+    c->M = (c->L + 1) * (c->L + 1);
+    c->nkx = c->N / 2 + 1;
+    c->nr = (int64_t)c->N * c->N * c->N;
+    c->nk = (int64_t)c->nkx * c->N * c->N;
+    c->fp32 = p->precision == WLC_FP32;
+    c->real4 = p->literals == WLC_LIT_REAL4 ? 1 : 0;
+    c->ds = 1.0 / (double)p->nmax;  // initialize_mod.f90:140
+    c->nstart[0] = 0;
+    c->nstart[1] = p->ns[0];
+    c->nstart[2] = p->ns[0] + p->ns[1];
+    *out = c;
+    if (!build_basis_tables(c->L, c->real4, c->tab, why)) return set_err(c, WLC_E_SELFTEST, why);
+    // shared-memory plan of the solve kernel
+    c->kc = 0;
+    for (int kc : {16, 8, 4, 2, 1}) {
+        if (kc > c->N) continue;
+        const size_t need = c->fp32 ? smem_solve<float>(c->N, c->M, c->L, kc) : smem_solve<double>(c->N, c->M, c->L, kc);
+        if (need <= 227 * 1024) {
+            c->kc = kc;
+            break;
+        }
+    }
+    const size_t sxy = c->fp32 ? smem_xy<float>(c->N) : smem_xy<double>(c->N);
+    if (c->kc == 0 || sxy > 227 * 1024)
+        return set_err(c, WLC_E_UNSUPPORTED, "one coefficient column (M x N) does not fit in shared memory for this "
+                                             "(N, L, precision)");
+    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    apply_box(c);
+    if ((rc = c->fp32 ? build_solve_tables<float>(c, c->sf) : build_solve_tables<double>(c, c->sd))) return rc;
+    // Theta and J lists
+    {
+        std::vector<int16_t> tr, tcol;
+        std::vector<double> tv;
+        const int M = c->M;
+        for (int i = 0; i < M; ++i)
+            for (int j = 0; j < M; ++j) {
+                bool any = false;
+                for (int a = 0; a < 5; ++a) any = any || c->tab.T[a][(size_t)i * M + j] != 0.0;
+                if (!any) continue;
+                tr.push_back((int16_t)i);
+                tcol.push_back((int16_t)j);
+                for (int a = 0; a < 5; ++a) tv.push_back(c->tab.T[a][(size_t)i * M + j]);
+            }
+        int16_t* p16;
+        double* pd;
+        if ((rc = upload(c, &p16, tr))) return rc;
+        c->thl.row = p16;
+        if ((rc = upload(c, &p16, tcol))) return rc;
+        c->thl.col = p16;
+        if ((rc = upload(c, &pd, tv))) return rc;
+        c->thl.val = pd;
+        c->thl.n = (int)tr.size();
+        std::vector<int> jp(6, 0);
+        std::vector<int16_t> jr, jc;
+        std::vector<double> jv;
+        for (int a = 0; a < 5; ++a) {
+            for (size_t e = 0; e < c->tab.Jsp[a].size(); ++e) {
+                jr.push_back((int16_t)c->tab.Jsp[a].row[e]);
+                jc.push_back((int16_t)c->tab.Jsp[a].col[e]);
+                jv.push_back(c->tab.Jsp[a].val[e]);
+            }
+            jp[a + 1] = (int)jv.size();
+        }
+        int* pi;
+        if ((rc = upload(c, &pi, jp))) return rc;
+        c->jl.ptr = pi;
+        if ((rc = upload(c, &p16, jr))) return rc;
+        c->jl.row = p16;
+        if ((rc = upload(c, &p16, jc))) return rc;
+        c->jl.col = p16;
+        if ((rc = upload(c, &pd, jv))) return rc;
+        c->jl.val = pd;
+    }
+    if ((rc = c->fp32 ? alloc_fields<float>(c) : alloc_fields<double>(c))) return rc;
+    const size_t nr = (size_t)c->nr;
+    if ((rc = dalloc(c, &c->w, sizeof(double) * 3 * nr))) return rc;
+    if ((rc = dalloc(c, &c->mop, sizeof(double) * 9 * nr))) return rc;
+    if ((rc = dalloc(c, &c->raw, sizeof(double) * 3 * nr))) return rc;
+    if ((rc = dalloc(c, &c->junc, sizeof(double) * 3 * nr))) return rc;
+    if ((rc = dalloc(c, &c->qend, sizeof(double) * nr))) return rc;
+    if ((rc = dalloc(c, &c->phi, sizeof(double) * 3 * nr))) return rc;
+    if ((rc = dalloc(c, &c->part, sizeof(double) * kS3Blocks))) return rc;
+    if ((rc = dalloc(c, &c->scal, sizeof(double) * 8))) return rc;
+    if ((rc = dalloc(c, &c->sraw, sizeof(double) * 15 * nr))) return rc;
+    if ((rc = dalloc(c, &c->ar, sizeof(double) * nr))) return rc;
+    if ((rc = dalloc(c, &c->stage, sizeof(double) * (size_t)c->M * nr))) return rc;
+    if ((rc = dalloc(c, &c->flag, sizeof(int)))) return rc;
+    CK(cudaMemsetAsync(c->mop, 0, sizeof(double) * 9 * nr, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->err.clear();
+    return WLC_OK;
+}
+
+extern "C" int wlc_destroy(wlc_ctx* c) {
+    if (!c) return WLC_OK;
+    if (c->st) cudaStreamSynchronize(c->st);
+    for (void* p : c->allocs) cudaFree(p);
+    for (auto e : c->ev) cudaEventDestroy(e);
+    if (c->st) cudaStreamDestroy(c->st);
+    delete c;
+    return WLC_OK;
+}
+
+static bool ready(wlc_ctx* c) { return c && c->st; }
+
+extern "C" int wlc_set_box(wlc_ctx* c, double dx, double dy, double dz) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!(dx > 0 && dy > 0 && dz > 0)) return set_err(c, WLC_E_PARAM, "grid spacing must be > 0");
+    c->p.dx[0] = dx;
+    c->p.dx[1] = dy;
+    c->p.dx[2] = dz;
+    apply_box(c);
+    c->have_fwd = c->have_bwd = c->have_density = false;
+    return WLC_OK;
+}
+
+extern "C" int wlc_set_fields(wlc_ctx* c, const double* w, const double* m_op) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!w) return set_err(c, WLC_E_PARAM, "w is null");
+    const size_t nr = (size_t)c->nr;
+    CK(cudaMemcpyAsync(c->w, w, sizeof(double) * 3 * nr, cudaMemcpyHostToDevice, c->st));
+    if (m_op) {
+        CK(cudaMemcpyAsync(c->mop, m_op, sizeof(double) * 9 * nr, cudaMemcpyHostToDevice, c->st));
+        c->have_mop = true;
+    } else {
+        CK(cudaMemsetAsync(c->mop, 0, sizeof(double) * 9 * nr, c->st));
+        c->have_mop = false;
+    }
+    const double third = lit_third(c->real4);
+    for (int b = 0; b < 3; ++b) {
+        if (c->fp32)
+            launch_make_cf<float>(c->w + b * nr, (float*)c->cf + (size_t)b * 3 * nr, c->ds, third, c->nr, c->st);
+        else
+            launch_make_cf<double>(c->w + b * nr, (double*)c->cf + (size_t)b * 3 * nr, c->ds, third, c->nr, c->st);
+        c->launches++;
+    }
+    CK(cudaGetLastError());
+    c->have_fields = true;
+    c->have_fwd = c->have_bwd = c->have_density = false;
+    return WLC_OK;
+}
+
+// (order, sigma, block) of one contour step
+struct StepKind {
+    int order, sigma, blk;
+};
+
+static int blk_fwd(const wlc_ctx* c, int s) {  // MDE_ABC.f90:44-57
+    if (s <= c->nstart[1]) return 0;
+    if (s <= c->nstart[2]) return 1;
+    return 2;
+}
+static int blk_bwd(const wlc_ctx* c, int s) {  // MDE_ABC.f90:69-83
+    if (s >= c->nstart[2]) return 2;
+    if (s >= c->nstart[1]) return 1;
+    return 0;
+}
+
+// Fill the launch description of one step.  h1..h3: history (or the RHS
+// for order 0), qout: destination slice.
+template <typename T>
+static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h2, const T* h3, T* qout) {
+    using C = typename cvec<T>::t;
+    StepLaunch<T> L;
+    const size_t nr = (size_t)c->nr;
+    StepArgs<T>& a = L.step;
+    a.h1 = h1;
+    a.h2 = h2;
+    a.h3 = h3;
+    a.wb = c->w + (size_t)k.blk * nr;
+    a.cf = (const T*)c->cf + (size_t)k.blk * 3 * nr;
+    a.msterm = nullptr;
+    a.order = k.order;
+    a.ds = (T)c->ds;
+    a.phat = (C*)c->phat;
+    a.twg = (const C*)c->twg;
+    a.M = c->M;
+    a.qout = qout;
+    a.minv = (T)(1.0 / (double)c->nr);  // M_grid_inv, wormlike_MDE_2dcomp_mod.f90:307
+    SolveArgs<T>& s = L.solve;
+    s.phat = (C*)c->phat;
+    s.twg = (const C*)c->twg;
+    if constexpr (sizeof(T) == 8)
+        s.tab = c->sd;
+    else
+        s.tab = c->sf;
+    for (int q = 0; q < 3; ++q) s.kf[q] = c->kf[q];
+    s.ds = c->ds;
+    const int ord = k.order == 0 ? 3 : k.order;
+    (void)ord;
+    s.sigma = k.sigma;
+    s.kc = c->kc;
+    s.nkx = c->nkx;
+    // diagonal of G (Gmatrix_2dcomp_mod.f90:394): c0 + ds*Loa*l(l+1)/(2 kappa)
+    s.dcoef = c->ds * c->p.loa / (2.0 * c->p.kappa[k.blk]);
+    return L;
+}
+
+template <typename T> static int run_step(wlc_ctx* c, StepLaunch<T>& L, double c0, int slot) {
+    L.solve.c0 = c0;
+    if (c->timing) L.events = &c->ev[4 * (size_t)slot];
+    cudaError_t e = launch_step<T>(c->N, L, c->st);
+    c->launches += 3;
+    if (e != cudaSuccess) return set_err(c, WLC_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
+    return WLC_OK;
+}
+
+template <typename T> static int sweep(wlc_ctx* c, int dir) {
+    const size_t sl = (size_t)c->M * c->nr;
+    T* q = (T*)(dir > 0 ? c->qf : c->qb);
+    const int nmax = c->p.nmax;
+    const bool ms = std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop;
+    if (c->timing && c->ev.size() < 4 * (size_t)(nmax + 1)) {
+        for (auto e : c->ev) cudaEventDestroy(e);
+        c->ev.assign(4 * (size_t)(nmax + 1), nullptr);
+        for (auto& e : c->ev) CK(cudaEventCreate(&e));
+    }
+    const int s_init = dir > 0 ? 0 : nmax;
+    launch_set_delta<T>(q + (size_t)s_init * sl, c->M, c->nr, c->st);  // q(0)=delta / q*(Nmax)=delta
+    c->launches++;
+    for (int n = 1; n <= nmax; ++n) {
+        const int s = dir > 0 ? n : nmax - n;
+        const int order = n < 3 ? n : 3;
+        StepKind k{order, dir, dir > 0 ? blk_fwd(c, s) : blk_bwd(c, s)};
+        const T* h1 = q + (size_t)(s - dir) * sl;
+        const T* h2 = order >= 2 ? q + (size_t)(s - 2 * dir) * sl : nullptr;
+        const T* h3 = order >= 3 ? q + (size_t)(s - 3 * dir) * sl : nullptr;
+        StepLaunch<T> L = make_launch<T>(c, k, h1, h2, h3, q + (size_t)s * sl);
+        if (ms) {
+            launch_ms_term<T>(h1, h2, h3, order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M, c->nr,
+                              (T*)c->msterm, c->st);
+            c->launches++;
+            L.step.msterm = (const T*)c->msterm;
+        }
+        int rc = run_step<T>(c, L, lit_c0(order, c->real4), n);
+        if (rc) return rc;
+    }
+    CK(cudaGetLastError());
+    if (c->timing) {
+        CK(cudaStreamSynchronize(c->st));
+        for (int q2 = 0; q2 < 4; ++q2) c->tms[q2] = 0.0;
+        for (int n = 1; n <= nmax; ++n) {
+            float t;
+            for (int q2 = 0; q2 < 3; ++q2) {
+                CK(cudaEventElapsedTime(&t, c->ev[4 * n + q2], c->ev[4 * n + q2 + 1]));
+                c->tms[q2] += t;
+            }
+            CK(cudaEventElapsedTime(&t, c->ev[4 * n], c->ev[4 * n + 3]));
+            c->tms[3] += t;
+        }
+    }
+    return WLC_OK;
+}
+
+extern "C" int wlc_propagate(wlc_ctx* c, int32_t dir) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (dir != 1 && dir != -1) return set_err(c, WLC_E_PARAM, "dir must be +1 or -1");
+    if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must be called before wlc_propagate");
+    int rc = c->fp32 ? sweep<float>(c, dir) : sweep<double>(c, dir);
+    if (rc) return rc;
+    if (dir > 0)
+        c->have_fwd = true;
+    else
+        c->have_bwd = true;
+    c->have_density = false;
+    return WLC_OK;
+}
+
+extern "C" int wlc_enable_timing(wlc_ctx* c, int32_t on) {
+    if (!ready(c)) return WLC_E_STATE;
+    c->timing = on != 0;
+    return WLC_OK;
+}
+
+extern "C" int wlc_last_timing(const wlc_ctx* c, double* ms4) {
+    if (!c || !ms4) return WLC_E_PARAM;
+    for (int q = 0; q < 4; ++q) ms4[q] = c->tms[q];
+    return WLC_OK;
+}
+
+template <typename T> static void density_launch(wlc_ctx* c, const DensityArgs& d) {
+    launch_density<T>((const T*)c->qf, (const T*)c->qb, d, c->raw, c->junc, c->qend, c->st);
+}
+template <typename T> static void stensor_launch(wlc_ctx* c, const DensityArgs& d) {
+    launch_stensor<T>((const T*)c->qf, (const T*)c->qb, d, c->jl, c->sraw, c->st);
+}
+
+extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, double* lnq) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!c->have_fwd || !c->have_bwd)
+        return set_err(c, WLC_E_STATE, "both sweeps (wlc_propagate +1 and -1) must precede wlc_density");
+    const size_t nr = (size_t)c->nr;
+    DensityArgs d;
+    d.nr = c->nr;
+    d.M = c->M;
+    d.nmax = c->p.nmax;
+    for (int b = 0; b < 3; ++b) {
+        d.nstart[b] = c->nstart[b];
+        d.ns[b] = c->p.ns[b];
+    }
+    d.ds = c->ds;
+    S3Args s3;
+    for (int a = 0; a < 3; ++a) {
+        s3.n[a] = c->N;
+        s3.d[a] = c->p.dx[a];
+    }
+    if (c->fp32)
+        density_launch<float>(c, d);
+    else
+        density_launch<double>(c, d);
+    launch_s3(c->qend, 1, 0, s3, c->part, c->scal + 0, c->st);          // S3(q_0(Nmax))
+    launch_s3(c->raw, 3, (int64_t)nr, s3, c->part, c->scal + 1, c->st);  // totden
+    CK(cudaMemcpyAsync(c->phi, c->raw, sizeof(double) * 3 * nr, cudaMemcpyDeviceToDevice, c->st));
+    launch_scale(c->phi, 3 * (int64_t)nr, c->scal + 1, c->vol, c->st);
+    launch_scale(c->junc, 3 * (int64_t)nr, c->scal + 1, c->vol, c->st);
+    c->launches += 7;
+    double hs[2];
+    CK(cudaMemcpyAsync(hs, c->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemsetAsync(c->flag, 0, sizeof(int), c->st));
+    launch_nonfinite(c->phi, 3 * (int64_t)nr, c->flag, c->st);
+    c->launches++;
+    int hflag = 0;
+    CK(cudaMemcpyAsync(&hflag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    if (phi) CK(cudaMemcpyAsync(phi, c->phi, sizeof(double) * 3 * nr, cudaMemcpyDeviceToHost, c->st));
+    if (junc) CK(cudaMemcpyAsync(junc, c->junc, sizeof(double) * 3 * nr, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->totden = hs[1];
+    c->lnq = std::log(hs[0] / c->vol);  // pff_global = ln[(1/V) S3(q_0)], SCFT_Density_FE_ABC.f90:82-92
+    if (lnq) *lnq = c->lnq;
+    if (hflag || !std::isfinite(c->lnq) || !std::isfinite(c->totden))
+        return set_err(c, WLC_E_NONFINITE, "non-finite density or partition function");
+    if (s_op) {
+        if (c->fp32)
+            stensor_launch<float>(c, d);
+        else
+            stensor_launch<double>(c, d);
+        launch_scale(c->sraw, 15 * (int64_t)nr, c->scal + 1, c->vol, c->st);
+        c->launches += 2;
+        std::vector<double> h(15 * nr);
+        CK(cudaMemcpyAsync(h.data(), c->sraw, sizeof(double) * 15 * nr, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        // S_OP_blk(r, a, b, blk) at s_op[r + nr*(a + 3b + 9 blk)]; S_zz = -S_xx - S_yy
+        for (int b = 0; b < 3; ++b)
+            for (size_t r = 0; r < nr; ++r) {
+                const double* t = h.data() + (size_t)b * 5 * nr + r;
+                const double sxx = t[0], syy = t[nr], sxy = t[2 * nr], sxz = t[3 * nr], syz = t[4 * nr];
+                const double S[9] = {sxx, sxy, sxz, sxy, syy, syz, sxz, syz, -(sxx + syy)};
+                for (int q = 0; q < 9; ++q) s_op[r + nr * (q + 9 * (size_t)b)] = S[q];
+            }
+    }
+    c->have_density = true;
+    return WLC_OK;
+}
+
+extern "C" int wlc_free_energy(wlc_ctx* c, double* fe) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!fe) return set_err(c, WLC_E_PARAM, "fe is null");
+    if (!c->have_density) return set_err(c, WLC_E_STATE, "wlc_density must precede wlc_free_energy");
+    FeArgs f;
+    f.nr = c->nr;
+    for (int a = 0; a < 3; ++a) f.chi[a] = c->p.chi[a];
+    f.nmu = c->p.nmu;
+    f.ms = (std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop) ? 1 : 0;
+    S3Args s3;
+    for (int a = 0; a < 3; ++a) {
+        s3.n[a] = c->N;
+        s3.d[a] = c->p.dx[a];
+    }
+    launch_fe(c->phi, c->w, c->mop, f, c->ar, c->st);
+    launch_s3(c->ar, 1, 0, s3, c->part, c->scal + 2, c->st);
+    c->launches += 3;
+    double h = 0;
+    CK(cudaMemcpyAsync(&h, c->scal + 2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    *fe = -c->lnq + h / c->vol;  // FE_global = -pff_global + tempEE_global
+    if (!std::isfinite(*fe)) return set_err(c, WLC_E_NONFINITE, "non-finite free energy");
+    return WLC_OK;
+}
+
+template <typename T> static int get_q(wlc_ctx* c, int dir, int s, double* out) {
+    const size_t sl = (size_t)c->M * c->nr;
+    const T* q = (const T*)(dir > 0 ? c->qf : c->qb) + (size_t)s * sl;
+    launch_to_reference<T>(q, c->stage, c->M, c->nr, c->st);
+    c->launches++;
+    CK(cudaMemcpyAsync(out, c->stage, sizeof(double) * sl, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return WLC_OK;
+}
+
+template <typename T> static int set_q(wlc_ctx* c, int dir, int s, const double* in) {
+    const size_t sl = (size_t)c->M * c->nr;
+    T* q = (T*)(dir > 0 ? c->qf : c->qb) + (size_t)s * sl;
+    CK(cudaMemcpyAsync(c->stage, in, sizeof(double) * sl, cudaMemcpyHostToDevice, c->st));
+    launch_to_internal<T>(c->stage, q, c->M, c->nr, c->st);
+    c->launches++;
+    CK(cudaStreamSynchronize(c->st));
+    return WLC_OK;
+}
+
+extern "C" int wlc_get_q(wlc_ctx* c, int32_t dir, int32_t s, double* out) {
+    if (!ready(c)) return WLC_E_STATE;
+    if ((dir != 1 && dir != -1) || s < 0 || s > c->p.nmax || !out)
+        return set_err(c, WLC_E_PARAM, "wlc_get_q: bad dir / s / out");
+    return c->fp32 ? get_q<float>(c, dir, s, out) : get_q<double>(c, dir, s, out);
+}
+
+extern "C" int wlc_set_q(wlc_ctx* c, int32_t dir, int32_t s, const double* in) {
+    if (!ready(c)) return WLC_E_STATE;
+    if ((dir != 1 && dir != -1) || s < 0 || s > c->p.nmax || !in)
+        return set_err(c, WLC_E_PARAM, "wlc_set_q: bad dir / s / in");
+    return c->fp32 ? set_q<float>(c, dir, s, in) : set_q<double>(c, dir, s, in);
+}
+
+template <typename T> static int init_pr_impl(wlc_ctx* c, int dir, int s, double* pr) {
+    const size_t sl = (size_t)c->M * c->nr;
+    T* q = (T*)(dir > 0 ? c->qf : c->qb);
+    const int n = dir > 0 ? s : c->p.nmax - s;
+    const int order = n < 3 ? n : 3;
+    StepKind k{order, dir, dir > 0 ? blk_fwd(c, s) : blk_bwd(c, s)};
+    const T* h1 = q + (size_t)(s - dir) * sl;
+    const T* h2 = order >= 2 ? q + (size_t)(s - 2 * dir) * sl : nullptr;
+    const T* h3 = order >= 3 ? q + (size_t)(s - 3 * dir) * sl : nullptr;
+    StepLaunch<T> L = make_launch<T>(c, k, h1, h2, h3, (T*)c->work);
+    if (std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop) {
+        launch_ms_term<T>(h1, h2, h3, order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M, c->nr, (T*)c->msterm,
+                          c->st);
+        c->launches++;
+        L.step.msterm = (const T*)c->msterm;
+    }
+    cudaError_t e = launch_rhs_only<T>(c->N, L.step, (T*)c->work, c->st);
+    c->launches++;
+    if (e != cudaSuccess) return set_err(c, WLC_E_CUDA, cudaGetErrorString(e));
+    launch_to_reference<T>((const T*)c->work, c->stage, c->M, c->nr, c->st);
+    c->launches++;
+    CK(cudaMemcpyAsync(pr, c->stage, sizeof(double) * sl, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return WLC_OK;
+}
+
+extern "C" int wlc_init_pr(wlc_ctx* c, int32_t dir, int32_t s, double* pr) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!pr || (dir != 1 && dir != -1)) return set_err(c, WLC_E_PARAM, "wlc_init_pr: bad dir / pr");
+    if ((dir > 0 && (s < 1 || s > c->p.nmax)) || (dir < 0 && (s < 0 || s > c->p.nmax - 1)))
+        return set_err(c, WLC_E_PARAM, "wlc_init_pr: s out of range");
+    if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must precede wlc_init_pr");
+    return c->fp32 ? init_pr_impl<float>(c, dir, s, pr) : init_pr_impl<double>(c, dir, s, pr);
+}
+
+// ABC G_index table, Gmatrix_mod-old.f90:446-518
+static bool g_index_kind(int g, StepKind& k) {
+    static const StepKind tab[10] = {{1, 1, 0}, {2, 1, 0}, {3, 1, 0}, {3, 1, 1}, {3, 1, 2},
+                                     {3, -1, 0}, {3, -1, 1}, {3, -1, 2}, {2, -1, 2}, {1, -1, 2}};
+    if (g < 1 || g > 10) return false;
+    k = tab[g - 1];
+    return true;
+}
+
+template <typename T> static int one_step_impl(wlc_ctx* c, StepKind k, const double* pr, double* qout) {
+    const size_t sl = (size_t)c->M * c->nr;
+    CK(cudaMemcpyAsync(c->stage, pr, sizeof(double) * sl, cudaMemcpyHostToDevice, c->st));
+    launch_to_internal<T>(c->stage, (T*)c->work, c->M, c->nr, c->st);
+    c->launches++;
+    StepKind k0 = k;
+    k0.order = 0;
+    StepLaunch<T> L = make_launch<T>(c, k0, (const T*)c->work, nullptr, nullptr, (T*)c->work);
+    int rc = run_step<T>(c, L, lit_c0(k.order, c->real4), 0);
+    if (rc) return rc;
+    launch_to_reference<T>((const T*)c->work, c->stage, c->M, c->nr, c->st);
+    c->launches++;
+    CK(cudaMemcpyAsync(qout, c->stage, sizeof(double) * sl, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return WLC_OK;
+}
+
+extern "C" int wlc_mde_one_step(wlc_ctx* c, int32_t g_index, const double* pr, double* q_out) {
+    if (!ready(c)) return WLC_E_STATE;
+    StepKind k;
+    if (!g_index_kind(g_index, k)) return set_err(c, WLC_E_PARAM, "G_index must be in 1..10");
+    if (!pr || !q_out) return set_err(c, WLC_E_PARAM, "null pr / q_out");
+    if (c->timing && c->ev.size() < 4) {
+        c->ev.assign(4, nullptr);
+        for (auto& e : c->ev) CK(cudaEventCreate(&e));
+    }
+    return c->fp32 ? one_step_impl<float>(c, k, pr, q_out) : one_step_impl<double>(c, k, pr, q_out);
+}

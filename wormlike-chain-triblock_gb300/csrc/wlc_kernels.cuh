@@ -1,0 +1,79 @@
+// wlc_kernels.cuh -- the three kernels of one contour step and their
+// arguments.  One BDF step of the reference (init_pr + mde_one_step,
+// MDE_ABC.f90:90-383; wormlike_MDE_2dcomp_mod.f90:323-455) runs as
+//   pass A  rhs_fft_xy : BDF right-hand side of one coefficient plane group,
+//                        R2C along x, C2C along y        -> phat[col][i][z]
+//   pass B  zfft_solve : per (kx, ky) column: C2C along z for every
+//                        coefficient, the per-k solve of G(k), inverse z
+//   pass C  ifft_xy    : inverse y, C2R along x, 1/N^3 -> q_s[i][r]
+// phat (the k-space intermediate) is laid out [col = ky*nkx + kx][i][z] so
+// that pass B reads one column as a single contiguous run.
+#pragma once
+#include <cstdint>
+
+#include "wlc_fft.cuh"
+
+namespace wlc {
+
+// z planes per CTA of passes A and C: 32-byte runs per (col, i) in phat,
+// fewer when the half-spectrum planes would not fit in shared memory
+__host__ __device__ constexpr int zg_planes(int N, int tsize) {
+    int z = 32 / (2 * tsize);
+    while (z > 1 && (size_t)(N + (N / 2) * N + z * N * (N / 2 + 1)) * 2 * tsize > 200 * 1024) z /= 2;
+    return z;
+}
+
+template <typename T> struct StepArgs {
+    using C = typename cvec<T>::t;
+    // pass A
+    const T* h1;        // history slices [M][nr] (q(s-1) / q*(s+1) ...), or Pr
+    const T* h2;
+    const T* h3;
+    const double* wb;   // block field [nr] (orders 1, 2)
+    const T* cf;        // order-3 coefficient planes [3][nr]
+    const T* msterm;    // optional ds*Theta*h term [M][nr] (Maier-Saupe) or null
+    int order;          // 0: h1 is the right-hand side itself; 1..3 BDF order
+    T ds;
+    C* phat;            // [nkx*N][M][N]
+    const C* twg;       // twiddle table exp(-2 pi i j/N), j < N
+    int M;
+    // pass C
+    T* qout;            // [M][nr]
+    T minv;             // 1/N^3
+};
+
+// Per-context constant data of the factorised solve (device pointers;
+// values in the compute type T).
+template <typename T> struct SolveTablesT {
+    int L, M;
+    int npairs;              // (l, m>0) pairs
+    const int16_t* pairs;    // [npairs][3]: index of (l, m), index of (l, -m), m
+    const int* xp_ptr;       // CSR of Xp over output rows
+    const int16_t* xp_col;
+    const T* xp_val;
+    const int* xm_ptr;       // CSR of Xm = Xp^T
+    const int16_t* xm_col;
+    const T* xm_val;
+    const T* zoff;           // [M] Rz coupling (l, m) -> (l+1, m)
+    int ndr;                 // correction entries (0: none)
+    const int* dr_ptr;       // CSR over rows
+    const int16_t* dr_col;
+    const int8_t* dr_axis;   // 0 x, 1 y, 2 z
+    const T* dr_val;
+};
+
+template <typename T> struct SolveArgs {
+    using C = typename cvec<T>::t;
+    C* phat;
+    const C* twg;
+    SolveTablesT<T> tab;
+    double kf[3];       // 2 pi / (SIDE * d) per axis
+    double ds;
+    double c0;          // BDF diagonal
+    double dcoef;       // ds * Loa / (2 kappa)
+    int sigma;          // +1 forward, -1 backward
+    int kc;             // k chunk (columns of the temp buffers)
+    int nkx;
+};
+
+}  // namespace wlc

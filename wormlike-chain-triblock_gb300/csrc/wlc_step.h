@@ -1,0 +1,35 @@
+// wlc_step.h -- host-side launch interface of the contour-step kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "wlc_kernels.cuh"
+
+// Grid edges with compiled kernels (cubic grids).
+#define WLC_FOR_EACH_N(X) X(8) X(12) X(16) X(24) X(32) X(40) X(48) X(64) X(96) X(128)
+
+namespace wlc {
+
+template <typename T> struct StepLaunch {
+    StepArgs<T> step;
+    SolveArgs<T> solve;
+    bool do_a = true, do_b = true, do_c = true;
+    cudaEvent_t* events = nullptr;  // 4 events around the three passes, or null
+};
+
+template <typename T> cudaError_t launch_step(int N, const StepLaunch<T>& s, cudaStream_t st);
+template <typename T> cudaError_t launch_rhs_only(int N, const StepArgs<T>& a, T* out, cudaStream_t st);
+template <typename T> size_t smem_xy(int N);
+template <typename T> size_t smem_solve(int N, int M, int L, int kc);
+
+inline bool supported_n(int n) {
+    switch (n) {
+#define WLC_CASE(v) case v:
+        WLC_FOR_EACH_N(WLC_CASE)
+#undef WLC_CASE
+        return true;
+        default:
+            return false;
+    }
+}
+
+}  // namespace wlc

@@ -1,0 +1,264 @@
+"""Python host mirror of the reference's propagator / density entry points,
+bound through the C ABI of libwlc.so (include/wlc.h) with ctypes.
+
+The reference (tjz2026/wormlike-chain-triblock) keeps its state in Fortran
+module globals and calls, per SCFT iteration (SCFT_control.f90:237-273):
+    calc_THETAij(); MDE_q(); MDE_qstar(); density(); free_energy()
+and, inside the ABC draft driver, init_pr(...) / mde_one_step(...)
+(MDE_ABC.f90:8-383) and init_inverse_sparse_GAB() on every box change
+(Gmatrix_2dcomp_mod.f90:222).  `Instance` exposes the same names on one
+GPU-resident instance.  There is no CPU fallback: if libwlc.so cannot be
+built or loaded, or no CUDA device exists, every call raises.
+
+Array layouts follow the reference's Fortran arrays (documented in wlc.h):
+propagator slices / right-hand sides are (nr, M) C arrays (coefficient
+fastest, as q_f(0:M-1, 0:LS, s)); fields are (3, nr); the Maier-Saupe
+tensor M_OP(0:LS,0:2,0:2) is a (3, 3, nr) C array indexed [b][a][r].
+Grid point r = x + nx*(y + ny*z).
+"""
+import ctypes
+import math
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+
+WLC_FP64, WLC_FP32 = 0, 1
+WLC_LIT_REAL4, WLC_LIT_REAL8 = 0, 1
+ERRORS = {-1: "WLC_E_PARAM", -2: "WLC_E_ALLOC", -3: "WLC_E_CUDA", -4: "WLC_E_STATE",
+          -5: "WLC_E_NONFINITE", -6: "WLC_E_UNSUPPORTED", -7: "WLC_E_SELFTEST"}
+
+# exported symbols declared in include/wlc.h
+SYMBOLS = ["wlc_abi_version", "wlc_create", "wlc_destroy", "wlc_last_error", "wlc_set_box",
+           "wlc_set_fields", "wlc_propagate", "wlc_density", "wlc_free_energy", "wlc_get_q",
+           "wlc_set_q", "wlc_init_pr", "wlc_mde_one_step", "wlc_launch_count", "wlc_stream",
+           "wlc_enable_timing", "wlc_last_timing"]
+
+
+class WlcError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Params(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int32 * 3), ("lmax", ctypes.c_int32), ("nmax", ctypes.c_int32),
+                ("ns", ctypes.c_int32 * 3), ("dx", ctypes.c_double * 3), ("loa", ctypes.c_double),
+                ("kappa", ctypes.c_double * 3), ("chi", ctypes.c_double * 3), ("nmu", ctypes.c_double),
+                ("precision", ctypes.c_int32), ("literals", ctypes.c_int32),
+                ("store_qstar", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+
+
+def lib_path():
+    return os.path.join(_HERE, "_lib", "libwlc.so")
+
+
+def load(build_if_missing=True):
+    """Load libwlc.so (building it in-tree when missing)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if build_if_missing:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_wlc_build", os.path.join(os.path.dirname(_HERE), "build.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = ctypes.CDLL(path)
+    P, I, D = ctypes.c_void_p, ctypes.c_int32, ctypes.c_double
+    Dp = ctypes.POINTER(ctypes.c_double)
+    lib.wlc_abi_version.restype = ctypes.c_int
+    lib.wlc_create.argtypes = [ctypes.POINTER(Params), ctypes.POINTER(P)]
+    lib.wlc_destroy.argtypes = [P]
+    lib.wlc_last_error.argtypes = [P]
+    lib.wlc_last_error.restype = ctypes.c_char_p
+    lib.wlc_set_box.argtypes = [P, D, D, D]
+    lib.wlc_set_fields.argtypes = [P, Dp, Dp]
+    lib.wlc_propagate.argtypes = [P, I]
+    lib.wlc_density.argtypes = [P, Dp, Dp, Dp, Dp]
+    lib.wlc_free_energy.argtypes = [P, Dp]
+    lib.wlc_get_q.argtypes = [P, I, I, Dp]
+    lib.wlc_set_q.argtypes = [P, I, I, Dp]
+    lib.wlc_init_pr.argtypes = [P, I, I, Dp]
+    lib.wlc_mde_one_step.argtypes = [P, I, Dp, Dp]
+    lib.wlc_launch_count.argtypes = [P]
+    lib.wlc_launch_count.restype = ctypes.c_int64
+    lib.wlc_stream.argtypes = [P]
+    lib.wlc_stream.restype = P
+    lib.wlc_enable_timing.argtypes = [P, I]
+    lib.wlc_last_timing.argtypes = [P, Dp]
+    _LIB = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+def even_block_lengths(f, nmax):
+    """Block lengths NA, NB, NC from fractions: the reference uses
+    NINT(f*Nmax) and stops unless all three are even
+    (initialize_mod.f90:142-144,190-195); here each of NA and NC is rounded
+    to the nearest even integer and NB takes the remainder (also even when
+    Nmax is even)."""
+    def ev(x):
+        return int(2 * math.floor(x / 2.0 + 0.5))
+    na = ev(f[0] * nmax)
+    nc = ev(f[2] * nmax) if len(f) > 2 else ev((1.0 - f[0] - f[1]) * nmax)
+    nb = nmax - na - nc
+    return na, nb, nc
+
+
+def wlc_radius_of_gyration(x):
+    """Rg / L for a wormlike chain of contour/persistence ratio x = L/lp."""
+    return math.sqrt(1.0 / (3.0 * x) - 1.0 / x ** 2 + 2.0 / x ** 3 - 2.0 / x ** 4 * (1.0 - math.exp(-x)))
+
+
+class Instance:
+    """One ABC-triblock instance on the current CUDA device."""
+
+    def __init__(self, n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_FP64,
+                 literals=WLC_LIT_REAL4):
+        self.lib = load()
+        p = Params()
+        n = (n, n, n) if np.isscalar(n) else tuple(n)
+        dx = (dx, dx, dx) if np.isscalar(dx) else tuple(dx)
+        p.n[:] = [int(v) for v in n]
+        p.lmax = int(lmax)
+        p.nmax = int(nmax)
+        p.ns[:] = [int(v) for v in ns]
+        p.dx[:] = [float(v) for v in dx]
+        p.loa = float(loa)
+        p.kappa[:] = [float(v) for v in kappa]
+        p.chi[:] = [float(v) for v in chi]
+        p.nmu = float(nmu)
+        p.precision = int(precision)
+        p.literals = int(literals)
+        p.store_qstar = 1
+        self.params = p
+        self.n = tuple(p.n)
+        self.nr = self.n[0] * self.n[1] * self.n[2]
+        self.M = (p.lmax + 1) ** 2
+        self.nmax = p.nmax
+        self.h = ctypes.c_void_p()
+        rc = self.lib.wlc_create(ctypes.byref(p), ctypes.byref(self.h))
+        if rc != 0:
+            msg = self.lib.wlc_last_error(self.h).decode() if self.h else ""
+            self.lib.wlc_destroy(self.h)
+            self.h = None
+            raise WlcError(rc, msg)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WlcError(rc, self.lib.wlc_last_error(self.h).decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wlc_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def volume(self):
+        d = self.params.dx
+        return d[0] * d[1] * d[2] * self.nr
+
+    @property
+    def launch_count(self):
+        return self.lib.wlc_launch_count(self.h)
+
+    @property
+    def stream(self):
+        return self.lib.wlc_stream(self.h)
+
+    # -------------------------------------------------- reference entry points
+    def init_inverse_sparse_GAB(self, dx=None):
+        """Box change: Gmatrix_2dcomp_mod.f90:222 (the k-space operator is
+        rebuilt from the new spacing)."""
+        if dx is not None:
+            d = (dx, dx, dx) if np.isscalar(dx) else tuple(dx)
+            self.params.dx[:] = [float(v) for v in d]
+        d = self.params.dx
+        self._check(self.lib.wlc_set_box(self.h, d[0], d[1], d[2]))
+
+    def set_fields(self, w, m_op=None):
+        w = np.ascontiguousarray(w, dtype=np.float64).reshape(3, self.nr)
+        self._w = w
+        if m_op is None:
+            self._check(self.lib.wlc_set_fields(self.h, _dp(w), None))
+        else:
+            m = np.ascontiguousarray(m_op, dtype=np.float64).reshape(9, self.nr)
+            self._m = m
+            self._check(self.lib.wlc_set_fields(self.h, _dp(w), _dp(m)))
+
+    def calc_THETAij(self):
+        """Theta(r) is built from M_OP inside every step on the device
+        (wormlike_MDE_2dcomp_mod.f90:5-110); nothing to precompute."""
+        return None
+
+    def MDE_q(self):
+        self._check(self.lib.wlc_propagate(self.h, 1))
+
+    def MDE_qstar(self):
+        self._check(self.lib.wlc_propagate(self.h, -1))
+
+    def ABC_melt_driver(self):
+        self.MDE_q()
+        self.MDE_qstar()
+
+    def density(self, want_s=False, want_junction=True):
+        phi = np.empty((3, self.nr))
+        junc = np.empty((3, self.nr)) if want_junction else None
+        sop = np.empty((3, 3, 3, self.nr)) if want_s else None
+        lnq = np.zeros(1)
+        self._check(self.lib.wlc_density(self.h, _dp(phi), _dp(junc) if want_junction else None,
+                                         _dp(sop) if want_s else None, _dp(lnq)))
+        out = dict(lnQ=float(lnq[0]), phi=phi)
+        if want_junction:
+            out["junction"] = junc
+        if want_s:
+            # sop[blk][b][a][r] = S_OP_blk(r, a, b, blk)
+            out["S"] = sop
+        return out
+
+    def free_energy(self):
+        fe = np.zeros(1)
+        self._check(self.lib.wlc_free_energy(self.h, _dp(fe)))
+        return float(fe[0])
+
+    def get_q(self, direction, s):
+        out = np.empty((self.nr, self.M))
+        self._check(self.lib.wlc_get_q(self.h, int(direction), int(s), _dp(out)))
+        return out
+
+    def set_q(self, direction, s, q):
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.nr, self.M)
+        self._check(self.lib.wlc_set_q(self.h, int(direction), int(s), _dp(q)))
+
+    def init_pr(self, direction, s):
+        out = np.empty((self.nr, self.M))
+        self._check(self.lib.wlc_init_pr(self.h, int(direction), int(s), _dp(out)))
+        return out
+
+    def mde_one_step(self, g_index, pr, out=None):
+        pr = np.ascontiguousarray(pr, dtype=np.float64).reshape(self.nr, self.M)
+        if out is None:
+            out = np.empty((self.nr, self.M))
+        self._check(self.lib.wlc_mde_one_step(self.h, int(g_index), _dp(pr), _dp(out)))
+        return out
+
+    def enable_timing(self, on=True):
+        self._check(self.lib.wlc_enable_timing(self.h, 1 if on else 0))
+
+    def last_timing(self):
+        t = np.zeros(4)
+        self._check(self.lib.wlc_last_timing(self.h, _dp(t)))
+        return t
