@@ -1,0 +1,356 @@
+#!/usr/bin/env python3
+"""Benchmark of the wormlike-chain MDE hot path on GB300.
+
+Workload (the single-GPU configuration of the headline metric): one ABC
+triblock instance, 64^3 grid, box edge 5.0 Rg, l <= 10 (121 real-harmonic
+coefficients), Ns = 200 (blocks 50/100/50), chiN = 18 for all pairs,
+contour/persistence = 2.0, seeded random fields w ~ N(0, 0.5^2).
+
+One bench step = one SCFT iteration's hot path: forward propagator sweep
+(MDE_q), backward sweep (MDE_qstar), densities + Q (density) and the free
+energy -- 2*Ns = 400 contour steps.  `value` is contour steps/s with the
+fields resident on the device; `e2e` is the same metric through the C ABI
+with the fields copied host->device (pinned) and the block densities copied
+back every step.  The propagator history (51 GB per direction in FP64) is far
+larger than L2, so no L2 flush is needed between steps.
+
+--impl reference times the CPU restatement of the reference's step (the
+reference itself cannot be built: no Fortran/MPI/FFTW/MKL and undefined
+routines) on the host cores, on a bounded sample of the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "wormlike-chain-triblock_gb300"))
+
+import numpy as np  # noqa: E402
+
+PEAKS_FILE = os.path.join(REPO, "MEASURED_PEAKS.json")
+FALLBACK_HBM = 6800.0
+
+
+def workload(precision):
+    import wlc
+    x = 2.0  # contour / persistence
+    rg = wlc.wlc_radius_of_gyration(x)  # Rg / L
+    box = 5.0 * rg
+    n, L, nmax = 64, 10, 200
+    ns = wlc.even_block_lengths((0.25, 0.50, 0.25), nmax)
+    kappa = 0.5  # kapa_A of the reference; Loa/kappa = L/lp
+    return dict(n=n, L=L, nmax=nmax, ns=ns, dx=box / n, loa=x * kappa, kappa=(kappa,) * 3,
+                chi=(18.0, 18.0, 18.0), box=box, precision=precision, w_sigma=0.5)
+
+
+def algorithmic_bytes(wl, bq):
+    """Per contour step: BDF3 history read (3 slices) + one slice written +
+    the block field: (3+1)*M*N^3*b_q + 8*N^3."""
+    M = (wl["L"] + 1) ** 2
+    nr = wl["n"] ** 3
+    return 4 * M * nr * bq + 8 * nr
+
+
+def pass_bytes(wl, bq):
+    """Minimal DRAM bytes of each pass of one step: A reads the history and
+    writes the k-space planes, B reads and writes them, C reads them and
+    writes the new slice."""
+    M = (wl["L"] + 1) ** 2
+    n = wl["n"]
+    nr = n ** 3
+    nk = (n // 2 + 1) * n * n
+    kspace = M * nk * 2 * bq
+    return {"A": 3 * M * nr * bq + 8 * nr + kspace, "B": 2 * kspace, "C": kspace + M * nr * bq}
+
+
+class ClockSampler:
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def load_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return FALLBACK_HBM, "fallback"
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def cpu_sample(wl, seconds_target=20.0, nthreads=None):
+    """Time the CPU restatement of one BDF3 contour step at this workload:
+    RHS, forward FFTs and inverse FFTs of all coefficients on the full grid;
+    the per-k G solve on a sample of wavevectors, scaled to all of them."""
+    sys.path.insert(0, os.path.join(REPO, "oracle"))
+    import oracle
+    nthreads = nthreads or os.cpu_count() or 1
+    n = wl["n"]
+    o = oracle.Oracle((n, n, n), wl["L"], 4, (2, 2, 0), (wl["dx"],) * 3, wl["loa"], wl["kappa"], wl["chi"],
+                      nthreads=nthreads)
+    rng = np.random.default_rng(11)
+    o.set_fields(rng.normal(0.0, wl["w_sigma"], size=(3, n ** 3)))
+    M = (wl["L"] + 1) ** 2
+    for s in range(3):
+        o.set_q(1, s, rng.random((M, n ** 3)))
+    nk_sample = 2048
+    stages, est = o.bench_step(nk_sample)
+    o.close()
+    return dict(steps_per_s=1.0 / est, stages=stages.tolist(), est_s=est, cores=nthreads, nk_sample=nk_sample,
+                nk=(n // 2 + 1) * n * n)
+
+
+def run_reference(args, wl):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    samples = []
+    for it in range(args.warmup + args.steps):
+        r = cpu_sample(wl)
+        if it >= args.warmup:
+            samples.append(r)
+    v = statistics.median([s["steps_per_s"] for s in samples])
+    r = samples[-1]
+    sample = ("one BDF3 contour step per bench step: RHS and all forward/inverse FFTs on the full 64^3 x 121 "
+              "grid, per-k dense LU solve on %d of %d wavevectors scaled to all (LU factors prebuilt, as the "
+              "reference precomputes G^-1)" % (r["nk_sample"], r["nk"]))
+    line = {"impl": "reference", "metric": "MDE contour steps/s (64^3, L=10, Ns=200, ABC)", "value": v,
+            "unit": "steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic (seeded N(0,0.5^2) fields)",
+            "config": {"workload": "ABC triblock 64^3, box 5.0 Rg, L=10 (M=121), Ns=200 (50/100/50), chiN=18, "
+                                   "L/lp=2.0", "precision": "fp64"},
+            "cpu_baseline": {"value": v, "unit": "steps/s", "cores": r["cores"], "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args, wl):
+    import torch
+    import wlc
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    inst = wlc.Instance(wl["n"], wl["L"], wl["nmax"], wl["ns"], wl["dx"], wl["loa"], wl["kappa"], wl["chi"],
+                        precision=wlc.WLC_FP64 if wl["precision"] == "fp64" else wlc.WLC_FP32)
+    nr = wl["n"] ** 3
+    rng = np.random.default_rng(1234 + rank)
+    w_host = torch.empty((3, nr), dtype=torch.float64).pin_memory()
+    w_host.numpy()[:] = rng.normal(0.0, wl["w_sigma"], size=(3, nr))
+    phi_host = torch.empty((3, nr), dtype=torch.float64).pin_memory()
+    stream = torch.cuda.ExternalStream(inst.stream, device=dev)
+    import ctypes
+    lib = inst.lib
+    h = inst.h
+    wp = ctypes.cast(w_host.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    php = ctypes.cast(phi_host.data_ptr(), ctypes.POINTER(ctypes.c_double))
+    lnq = np.zeros(1)
+    lnqp = lnq.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+    fe = np.zeros(1)
+    fep = fe.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+    def check(rc):
+        if rc != 0:
+            raise RuntimeError(lib.wlc_last_error(h).decode())
+
+    def device_step():
+        check(lib.wlc_propagate(h, 1))
+        check(lib.wlc_propagate(h, -1))
+        check(lib.wlc_density(h, None, None, None, lnqp))
+
+    def e2e_step():
+        check(lib.wlc_set_fields(h, wp, None))
+        check(lib.wlc_propagate(h, 1))
+        check(lib.wlc_propagate(h, -1))
+        check(lib.wlc_density(h, php, None, None, lnqp))
+        check(lib.wlc_free_energy(h, fep))
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+            torch.cuda.synchronize()
+
+    check(lib.wlc_set_fields(h, wp, None))
+    for _ in range(args.warmup):
+        device_step()
+    barrier()
+    # ---- timed: device-resident
+    inst.enable_timing(True)
+    clk = ClockSampler(local)
+    clk.start()
+    l0 = inst.launch_count
+    ev = []
+    pass_ms = np.zeros(4)
+    t_wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        device_step()
+        e.record(stream)
+        ev.append((s, e))
+        pass_ms += inst.last_timing()  # per-sweep sums of the last (backward) sweep only
+    barrier()
+    t_wall = time.perf_counter() - t_wall0
+    clocks = clk.stop()
+    launches = inst.launch_count - l0
+    ms = [s.elapsed_time(e) for s, e in ev]
+    ms_total = float(sum(ms))
+    inst.enable_timing(False)
+    if world > 1:
+        t = torch.tensor([ms_total], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    steps_per_bench = 2 * wl["nmax"]
+    value = world * steps_per_bench * args.steps / (ms_total / 1000.0)
+    # ---- timed: end to end through the C ABI with host buffers
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    barrier()
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = world * steps_per_bench * args.steps / e2e_s
+    # ---- roofline of the dominant pass (pass times are of one sweep of Ns steps)
+    bq = 8 if wl["precision"] == "fp64" else 4
+    pb = pass_bytes(wl, bq)
+    per_pass = {"A": pass_ms[0], "B": pass_ms[1], "C": pass_ms[2]}
+    dom = max(per_pass, key=per_pass.get)
+    launches_per_sweep = args.steps * wl["nmax"]
+    avg_ms = per_pass[dom] / launches_per_sweep
+    peak, peak_kind = load_peaks()
+    achieved = pb[dom] / (avg_ms / 1000.0) / 1e9
+    step_ms = ms_total / (args.steps * steps_per_bench)
+    b_step = algorithmic_bytes(wl, bq)
+    pass_names = {"A": "rhs_fft_xy", "B": "zfft_solve", "C": "ifft_xy"}
+    share = {pass_names[k]: per_pass[k] / max(1e-9, sum(per_pass.values())) for k in per_pass}
+    traffic = None
+    tfile = os.path.join(REPO, "profiles", "traffic.json")
+    if os.path.exists(tfile):
+        try:
+            with open(tfile) as f:
+                tj = json.load(f)
+            traffic = tj.get(wl["precision"], {}).get(pass_names[dom])
+        except Exception:
+            traffic = None
+    roofline = {"bound": "hbm", "kernel": pass_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                "bytes_per_launch": pb[dom], "avg_launch_ms": avg_ms, "kernel_share": share,
+                "step": {"algorithmic_bytes": b_step, "ms": step_ms,
+                         "achieved_gbs": b_step / (step_ms / 1000.0) / 1e9,
+                         "frac": b_step / (step_ms / 1000.0) / 1e9 / peak}}
+    h2d = 3 * nr * 8
+    d2h = 3 * nr * 8 + 16
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        r = cpu_sample(wl)
+        cpu = {"value": r["steps_per_s"], "unit": "steps/s", "cores": r["cores"], "kind": "port",
+               "sample": "one BDF3 contour step at this workload (RHS + FFTs full grid, per-k LU solve on "
+                         "%d of %d wavevectors, scaled)" % (r["nk_sample"], r["nk"])}
+    if rank == 0:
+        line = {"metric": "MDE contour steps/s (64^3, L=10, Ns=200, ABC)", "value": value, "unit": "steps/s",
+                "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": ms_total / args.steps, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64" if wl["precision"] == "fp64" else "f32",
+                "data": "synthetic (seeded N(0,0.5^2) fields)",
+                "config": {"workload": "ABC triblock 64^3, box 5.0 Rg, L=10 (M=121), Ns=200 (50/100/50), chiN=18, "
+                                       "L/lp=2.0; one bench step = forward + backward sweep + densities "
+                                       "(400 contour steps)",
+                           "precision": wl["precision"], "l2": "inputs larger than L2 (51 GB history/direction)",
+                           "parallelism": "replicas" if world > 1 else "single"},
+                "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
+                "wall_s": t_wall}
+        print(json.dumps(line))
+    inst.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    args = ap.parse_args()
+    wl = workload(args.precision)
+    if args.impl == "reference":
+        run_reference(args, wl)
+    else:
+        run_ours(args, wl)
+
+
+if __name__ == "__main__":
+    main()

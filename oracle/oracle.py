@@ -69,6 +69,7 @@ def _load():
     lib.orc_simpson3.restype = D
     lib.orc_fft_r2c.argtypes = [P, Dp, Dp]
     lib.orc_fft_c2r.argtypes = [P, Dp, Dp]
+    lib.orc_bench_step.argtypes = [P, Int, Dp]
     lib.orc_three_j.argtypes = [Int] * 6
     lib.orc_three_j.restype = D
     lib.orc_triple_product.argtypes = [Int] * 7
@@ -188,6 +189,14 @@ class Oracle:
     def simpson3(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.nr)
         return self.lib.orc_simpson3(self.h, _dp(a))
+
+    def bench_step(self, nk_sample):
+        """Timed BDF3 step with the per-k solve sampled on nk_sample
+        wavevectors; returns (stage seconds[4], full-step estimate)."""
+        t = np.zeros(4)
+        self.lib.orc_bench_step(self.h, int(nk_sample), _dp(t))
+        est = t[0] + t[1] + t[2] * self.nk / max(1, min(nk_sample, self.nk)) + t[3]
+        return t, est
 
     def fft_r2c(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.nr)

@@ -961,3 +961,71 @@ double orc_free_energy(orc_ctx* c, double lnq, const double* phi) {
     free(ar);
     return -lnq + e;
 }
+
+/* ------------------------------------------------------------------ */
+/* Bounded timing sample of one BDF3 contour step (CPU baseline)         */
+/* ------------------------------------------------------------------ */
+
+static double now_s(void) {
+#ifdef _OPENMP
+    return omp_get_wtime();
+#else
+    return 0.0;
+#endif
+}
+
+/* One BDF3 forward step at slice s=3 from slices 0..2 with every stage run
+ * on the full grid except the per-k solve, which runs for the first
+ * `nk_sample` wavevectors only (their LU factors, which the reference
+ * precomputes once per box, are built outside the timed stages).
+ * t[0] rhs, t[1] forward FFTs, t[2] sampled solve, t[3] inverse FFTs
+ * (seconds).  The full-step estimate is t0 + t1 + t2*nk/nk_sample + t3. */
+void orc_bench_step(orc_ctx* c, int nk_sample, double* t) {
+    int M = c->M;
+    size_t nr = c->nr, nk = c->nk, sl = (size_t)M * nr;
+    if (nk_sample > (int)nk) nk_sample = (int)nk;
+    double* pr = (double*)malloc(sizeof(double) * sl);
+    cplx* P = (cplx*)malloc(sizeof(cplx) * nk * M);
+    cplx* lu = (cplx*)malloc(sizeof(cplx) * (size_t)nk_sample * M * M);
+    int* piv = (int*)malloc(sizeof(int) * (size_t)nk_sample * M);
+#pragma omp parallel for num_threads(c->nthreads)
+    for (int kk = 0; kk < nk_sample; ++kk) {
+        build_G(c, kk, 3, c->kappa[0], lu + (size_t)kk * M * M);
+        lu_factor(lu + (size_t)kk * M * M, piv + (size_t)kk * M, M);
+    }
+    double t0 = now_s();
+    rhs(c, 3, c->qf + 2 * sl, c->qf + 1 * sl, c->qf, c->w, pr);
+    double t1 = now_s();
+#pragma omp parallel num_threads(c->nthreads)
+    {
+        cplx* work = (cplx*)malloc(sizeof(cplx) * 1024);
+#pragma omp for
+        for (int i = 0; i < M; ++i) r2c3(c, pr + (size_t)i * nr, P + (size_t)i * nk, work);
+        free(work);
+    }
+    double t2 = now_s();
+#pragma omp parallel for num_threads(c->nthreads)
+    for (int kk = 0; kk < nk_sample; ++kk) {
+        cplx b[512];
+        for (int i = 0; i < M; ++i) b[i] = P[(size_t)i * nk + kk];
+        lu_solve(lu + (size_t)kk * M * M, piv + (size_t)kk * M, M, b);
+        for (int i = 0; i < M; ++i) P[(size_t)i * nk + kk] = b[i];
+    }
+    double t3 = now_s();
+#pragma omp parallel num_threads(c->nthreads)
+    {
+        cplx* work = (cplx*)malloc(sizeof(cplx) * 1024);
+#pragma omp for
+        for (int i = 0; i < M; ++i) c2r3(c, P + (size_t)i * nk, c->qf + 3 * sl + (size_t)i * nr, work);
+        free(work);
+    }
+    double t4 = now_s();
+    t[0] = t1 - t0;
+    t[1] = t2 - t1;
+    t[2] = t3 - t2;
+    t[3] = t4 - t3;
+    free(pr);
+    free(P);
+    free(lu);
+    free(piv);
+}
