@@ -121,3 +121,44 @@ def test_box_change_rebuilds_operator():
     rng = np.random.default_rng(5)
     pr = rng.standard_normal((g.M, g.nr))
     assert rel(g.mde_one_step(3, pr.T.copy()).T, o.one_step(3, 1, 0, pr)) < TOL64
+
+
+def _symmetric_traceless_mop(rng, nr, amp=0.3):
+    a = rng.normal(0.0, amp, size=(3, 3, nr))
+    m = 0.5 * (a + a.transpose(1, 0, 2))
+    tr = (m[0, 0] + m[1, 1] + m[2, 2]) / 3.0
+    for k in range(3):
+        m[k, k] -= tr
+    return m
+
+
+@pytest.mark.parametrize("lit", [wlc.WLC_LIT_REAL4, wlc.WLC_LIT_REAL8])
+def test_maier_saupe_sweeps(lit):
+    """Theta(r) coupling (calc_THETAij + the Theta term of init_pr) with a
+    seeded symmetric traceless M_OP, NMu != 0."""
+    n, L, nmax, ns = 8, 4, 8, (2, 4, 2)
+    dx = 1.0 / n
+    nmu = 5.0
+    g = wlc.Instance(n, L, nmax, ns, dx, 1.1, (0.5, 0.5, 0.5), (15.0, 15.0, 15.0), nmu=nmu, literals=lit)
+    o = oracle.Oracle((n, n, n), L, nmax, ns, (dx, dx, dx), 1.1, (0.5, 0.5, 0.5), (15.0, 15.0, 15.0), nmu=nmu,
+                      real4=1 if lit == wlc.WLC_LIT_REAL4 else 0)
+    rng = np.random.default_rng(21)
+    w = rng.normal(0.0, 0.5, size=(3, n ** 3))
+    mop = _symmetric_traceless_mop(rng, n ** 3)
+    g.set_fields(w, mop)
+    o.set_fields(w, mop.reshape(9, -1))
+    g.MDE_q()
+    g.MDE_qstar()
+    o.propagate(1)
+    o.propagate(-1)
+    for s in (1, 2, 5, nmax):
+        assert rel(g.get_q(1, s).T, o.get_q(1, s)) < TOL64
+    assert rel(g.init_pr(-1, 3).T, o.init_pr(-1, 3)) < TOL64
+    d = g.density(want_s=True)
+    od = o.density(want_s=True)
+    assert abs(d["lnQ"] - od["lnQ"]) <= TOL64 * max(1.0, abs(od["lnQ"]))
+    assert rel(d["phi"], od["phi"]) < TOL64
+    assert rel(d["S"].reshape(3, 9, -1), od["S"]) < TOL64
+    fe = g.free_energy()
+    ofe = o.free_energy(od["lnQ"], od["phi"])
+    assert abs(fe - ofe) <= TOL64 * abs(ofe)
