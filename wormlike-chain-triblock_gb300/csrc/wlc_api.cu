@@ -406,14 +406,13 @@ extern "C" int wlc_set_fields(wlc_ctx* c, const double* w, const double* m_op) {
         CK(cudaMemsetAsync(c->mop, 0, sizeof(double) * 9 * nr, c->st));
         c->have_mop = false;
     }
+    // one launch covers the three blocks: cf[blk][3][nr] from w[blk][nr]
     const double third = lit_third(c->real4);
-    for (int b = 0; b < 3; ++b) {
-        if (c->fp32)
-            launch_make_cf<float>(c->w + b * nr, (float*)c->cf + (size_t)b * 3 * nr, c->ds, third, c->nr, c->st);
-        else
-            launch_make_cf<double>(c->w + b * nr, (double*)c->cf + (size_t)b * 3 * nr, c->ds, third, c->nr, c->st);
-        c->launches++;
-    }
+    if (c->fp32)
+        launch_make_cf<float>(c->w, (float*)c->cf, c->ds, third, c->nr, c->st);
+    else
+        launch_make_cf<double>(c->w, (double*)c->cf, c->ds, third, c->nr, c->st);
+    c->launches++;
     CK(cudaGetLastError());
     c->have_fields = true;
     c->have_fwd = c->have_bwd = c->have_density = false;
