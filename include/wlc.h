@@ -128,6 +128,20 @@ int wlc_init_pr(wlc_ctx* ctx, int32_t dir, int32_t s, double* pr);
  * 7 GB3*, 8 GC3*, 9 GC2*, 10 GC1*).  pr, q_out: [r*M + i] host arrays. */
 int wlc_mde_one_step(wlc_ctx* ctx, int32_t g_index, const double* pr, double* q_out);
 
+/* No counterpart in the reference.  wlc_mde_one_step for callers that
+ * cannot allocate device memory (code handed only device pointers by its
+ * framework, fixed memory pools, driver-level plugins): FP64 only, no
+ * context, nothing allocated.  pr_dev / q_out_dev are DEVICE arrays in the
+ * coefficient-major layout [i*nr + r] (may alias).  The k-space scratch and
+ * operator tables live in one static 64 MiB device array per GPU, so sizes
+ * needing more (M * (N/2+1) * N^2 * 16 bytes plus ~100 kB of tables) are
+ * rejected with WLC_E_UNSUPPORTED.  The first call on a device looks up the
+ * array's address and uploads the tables: make it before any stream
+ * capture.  All calls share the array; calls that overlap on the GPU race.
+ * stream: cudaStream_t or NULL; errbuf (may be NULL) receives a message. */
+int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, const double* pr_dev, double* q_out_dev,
+                             void* stream, char* errbuf, int32_t errlen);
+
 /* Number of the library's own kernel launches issued on the context's
  * stream since creation (instrumentation). */
 int64_t wlc_launch_count(const wlc_ctx* ctx);
