@@ -139,6 +139,22 @@ def dist_setup(args):
     return world, rank, local
 
 
+def replica_throughput(units_local, seconds_local, group=None):
+    """Whole-job throughput of independent replicas: units summed over
+    ranks divided by the slowest rank's time (max over ranks)."""
+    import torch
+    import torch.distributed as dist
+    if group is None and not (dist.is_available() and dist.is_initialized()):
+        return units_local / seconds_local, units_local, seconds_local
+    u = torch.tensor([float(units_local)], dtype=torch.float64)
+    t = torch.tensor([float(seconds_local)], dtype=torch.float64)
+    if dist.get_backend(group) == "nccl":
+        u, t = u.cuda(), t.cuda()
+    dist.all_reduce(u, op=dist.ReduceOp.SUM, group=group)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX, group=group)
+    return float(u.item()) / float(t.item()), float(u.item()), float(t.item())
+
+
 def cpu_sample(wl, seconds_target=20.0, nthreads=None):
     """Time the CPU restatement of one BDF3 contour step at this workload:
     RHS, forward FFTs and inverse FFTs of all coefficients on the full grid;
@@ -262,12 +278,9 @@ def run_ours(args, wl):
     ms = [s.elapsed_time(e) for s, e in ev]
     ms_total = float(sum(ms))
     inst.enable_timing(False)
-    if world > 1:
-        t = torch.tensor([ms_total], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
     steps_per_bench = 2 * wl["nmax"]
-    value = world * steps_per_bench * args.steps / (ms_total / 1000.0)
+    value, _, t_max = replica_throughput(steps_per_bench * args.steps, ms_total / 1000.0)
+    ms_total = t_max * 1000.0
     # ---- timed: end to end through the C ABI with host buffers
     barrier()
     t0 = time.perf_counter()
@@ -275,11 +288,7 @@ def run_ours(args, wl):
         e2e_step()
     barrier()
     e2e_s = time.perf_counter() - t0
-    if world > 1:
-        t = torch.tensor([e2e_s], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = world * steps_per_bench * args.steps / e2e_s
+    e2e, _, e2e_s = replica_throughput(steps_per_bench * args.steps, e2e_s)
     # ---- roofline of the dominant pass (pass times are of one sweep of Ns steps)
     bq = 8 if wl["precision"] == "fp64" else 4
     pb = pass_bytes(wl, bq)

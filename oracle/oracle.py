@@ -115,6 +115,7 @@ class Oracle:
         self.h = lib.orc_create(n3, self.L, self.nmax, ns3, dx3, float(loa), k3, c3, float(nmu),
                                 int(real4), self.nthreads)
         self.dx = tuple(float(v) for v in dx)
+        self._loa = float(loa)
 
     def close(self):
         if self.h:
