@@ -345,6 +345,24 @@ def run_ours(args, wl):
         torch.distributed.destroy_process_group()
 
 
+def run_profile_case(args):
+    """Small-footprint case for ncu captures: the headline kernels (64^3,
+    L=10) on a 6-step chain (2/2/2), two forward and one backward sweep, a
+    density pass; a few GB of device memory."""
+    import wlc
+    wl = workload(args.precision)
+    inst = wlc.Instance(wl["n"], wl["L"], 6, (2, 2, 2), wl["dx"], wl["loa"], wl["kappa"], wl["chi"],
+                        precision=wlc.WLC_FP64 if args.precision == "fp64" else wlc.WLC_FP32)
+    rng = np.random.default_rng(5)
+    inst.set_fields(rng.normal(0.0, wl["w_sigma"], size=(3, wl["n"] ** 3)))
+    inst.MDE_q()
+    inst.MDE_q()
+    inst.MDE_qstar()
+    d = inst.density()
+    print(json.dumps({"profile_case": args.precision, "lnQ": d["lnQ"], "launches": inst.launch_count}))
+    inst.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -353,7 +371,11 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--profile", action="store_true", help="small-footprint case for ncu captures")
     args = ap.parse_args()
+    if args.profile:
+        run_profile_case(args)
+        return
     wl = workload(args.precision)
     if args.impl == "reference":
         run_reference(args, wl)

@@ -23,7 +23,9 @@ struct wlc_ctx {
     int real4 = 1;
     double ds = 0, vol = 0, kf[3] = {0, 0, 0};
     int nstart[3] = {0, 0, 0};
-    int kc = 1;
+    void* pivtab = nullptr;  // [order 1..3][blk][key][npiv] compute type, isotropic spacing only
+    int nkeys = 0, npiv = 0;
+    bool have_piv = false;
     cudaStream_t st = nullptr;
     std::string err;
     BasisTables tab;
@@ -104,7 +106,10 @@ template <typename T> static int build_solve_tables(wlc_ctx* c, SolveTablesT<T>&
             pairs.push_back((int16_t)m);
         }
     s.npairs = (int)pairs.size() / 3;
+    s.nnz = (int)t.xp_val.size();
     auto cvt = [](const std::vector<double>& v) { return std::vector<T>(v.begin(), v.end()); };
+    auto cvf = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
+    float* pf;
     auto i16 = [](const std::vector<int>& v) {
         std::vector<int16_t> o(v.size());
         for (size_t k = 0; k < v.size(); ++k) o[k] = (int16_t)v[k];
@@ -122,14 +127,20 @@ template <typename T> static int build_solve_tables(wlc_ctx* c, SolveTablesT<T>&
     s.xp_col = p16;
     if ((rc = upload(c, &pv, cvt(t.xp_val)))) return rc;
     s.xp_val = pv;
+    if ((rc = upload(c, &pf, cvf(t.xp_val)))) return rc;
+    s.xp_valf = pf;
     if ((rc = upload(c, &pi, t.xm_ptr))) return rc;
     s.xm_ptr = pi;
     if ((rc = upload(c, &p16, i16(t.xm_col)))) return rc;
     s.xm_col = p16;
     if ((rc = upload(c, &pv, cvt(t.xm_val)))) return rc;
     s.xm_val = pv;
+    if ((rc = upload(c, &pf, cvf(t.xm_val)))) return rc;
+    s.xm_valf = pf;
     if ((rc = upload(c, &pv, cvt(t.zoff)))) return rc;
     s.zoff = pv;
+    if ((rc = upload(c, &pf, cvf(t.zoff)))) return rc;
+    s.zofff = pf;
     // correction entries, CSR over rows
     std::vector<std::vector<std::pair<int, std::pair<int, double>>>> rows(t.M);
     for (int a = 0; a < 3; ++a)
@@ -138,12 +149,12 @@ template <typename T> static int build_solve_tables(wlc_ctx* c, SolveTablesT<T>&
     std::vector<int> ptr(t.M + 1, 0);
     std::vector<int16_t> col;
     std::vector<int8_t> axis;
-    std::vector<T> val;
+    std::vector<float> val;
     for (int i = 0; i < t.M; ++i) {
         for (auto& e : rows[i]) {
             col.push_back((int16_t)e.first);
             axis.push_back((int8_t)e.second.first);
-            val.push_back((T)e.second.second);
+            val.push_back((float)e.second.second);
         }
         ptr[i + 1] = (int)val.size();
     }
@@ -155,8 +166,8 @@ template <typename T> static int build_solve_tables(wlc_ctx* c, SolveTablesT<T>&
     s.dr_col = p16;
     if ((rc = upload(c, &p8, axis))) return rc;
     s.dr_axis = p8;
-    if ((rc = upload(c, &pv, val))) return rc;
-    s.dr_val = pv;
+    if ((rc = upload(c, &pf, val))) return rc;
+    s.dr_valf = pf;
     return WLC_OK;
 }
 
@@ -239,6 +250,26 @@ static void apply_box(wlc_ctx* c) {
     c->vol = c->p.dx[0] * c->p.dx[1] * c->p.dx[2] * (double)c->nr;  // SCFT_control.f90:180
 }
 
+// Inverse tridiagonal pivots for every (order, block) when the spacing is
+// isotropic (|k|^2 then depends on ix^2+iy^2+iz^2 only).
+template <typename T> static int build_pivots(wlc_ctx* c) {
+    c->have_piv = false;
+    if (!c->pivtab) return WLC_OK;
+    if (!(c->kf[0] == c->kf[1] && c->kf[1] == c->kf[2])) return WLC_OK;
+    const T* zoff = sizeof(T) == 8 ? (const T*)c->sd.zoff : (const T*)c->sf.zoff;
+    for (int order = 1; order <= 3; ++order)
+        for (int b = 0; b < 3; ++b) {
+            T* out = (T*)c->pivtab + ((size_t)((order - 1) * 3 + b) * c->nkeys) * c->npiv;
+            const double dcoef = c->ds * c->p.loa / (2.0 * c->p.kappa[b]);
+            cudaError_t e = launch_pivot_table<T>(out, c->nkeys, c->L, lit_c0(order, c->real4), dcoef, c->ds, c->kf[0],
+                                                  zoff, c->st);
+            c->launches++;
+            if (e != cudaSuccess) return set_err(c, WLC_E_CUDA, std::string("pivot table: ") + cudaGetErrorString(e));
+        }
+    c->have_piv = true;
+    return WLC_OK;
+}
+
 template <typename T> static int alloc_fields(wlc_ctx* c) {
     using C = typename cvec<T>::t;
     const size_t sl = (size_t)c->M * c->nr;
@@ -290,20 +321,18 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
     c->nstart[2] = p->ns[0] + p->ns[1];
     *out = c;
     if (!build_basis_tables(c->L, c->real4, c->tab, why)) return set_err(c, WLC_E_SELFTEST, why);
-    // shared-memory plan of the solve kernel
-    c->kc = 0;
-    for (int kc : {16, 8, 4, 2, 1}) {
-        if (kc > c->N) continue;
-        const size_t need = c->fp32 ? smem_solve<float>(c->N, c->M, c->L, kc) : smem_solve<double>(c->N, c->M, c->L, kc);
-        if (need <= 227 * 1024) {
-            c->kc = kc;
-            break;
-        }
-    }
     const size_t sxy = c->fp32 ? smem_xy<float>(c->N) : smem_xy<double>(c->N);
-    if (c->kc == 0 || sxy > 227 * 1024)
-        return set_err(c, WLC_E_UNSUPPORTED, "one coefficient column (M x N) does not fit in shared memory for this "
-                                             "(N, L, precision)");
+    {
+        int npairs = c->L * (c->L + 1) / 2, ndr = 0;
+        for (int a = 0; a < 3; ++a) ndr += (int)c->tab.dR[a].size();
+        const bool corr = !c->fp32 && ndr > 0;
+        const size_t ssv = solve_smem(c->N, c->M, c->L, 8, npairs, (int)c->tab.xp_val.size(), ndr,
+                                      c->fp32 ? 4 : 8, corr ? 1 : 0)
+                               .total;
+        if (ssv > 227 * 1024 || sxy > 227 * 1024)
+            return set_err(c, WLC_E_UNSUPPORTED, "one coefficient column (M x N) does not fit in shared memory for "
+                                                 "this (N, L, precision)");
+    }
     CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
     apply_box(c);
     if ((rc = c->fp32 ? build_solve_tables<float>(c, c->sf) : build_solve_tables<double>(c, c->sd))) return rc;
@@ -352,6 +381,14 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
         c->jl.val = pd;
     }
     if ((rc = c->fp32 ? alloc_fields<float>(c) : alloc_fields<double>(c))) return rc;
+    c->nkeys = 3 * (c->N / 2) * (c->N / 2) + 1;
+    c->npiv = (c->L + 1) * (c->L + 2) / 2;
+    {
+        void* pv = nullptr;
+        if ((rc = dalloc(c, (unsigned char**)&pv, (size_t)9 * c->nkeys * c->npiv * (c->fp32 ? 4 : 8)))) return rc;
+        c->pivtab = pv;
+    }
+    if ((rc = c->fp32 ? build_pivots<float>(c) : build_pivots<double>(c))) return rc;
     const size_t nr = (size_t)c->nr;
     if ((rc = dalloc(c, &c->w, sizeof(double) * 3 * nr))) return rc;
     if ((rc = dalloc(c, &c->mop, sizeof(double) * 9 * nr))) return rc;
@@ -390,6 +427,8 @@ extern "C" int wlc_set_box(wlc_ctx* c, double dx, double dy, double dz) {
     c->p.dx[1] = dy;
     c->p.dx[2] = dz;
     apply_box(c);
+    int rc = c->fp32 ? build_pivots<float>(c) : build_pivots<double>(c);
+    if (rc) return rc;
     c->have_fwd = c->have_bwd = c->have_density = false;
     return WLC_OK;
 }
@@ -465,11 +504,13 @@ static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h
         s.tab = c->sf;
     for (int q = 0; q < 3; ++q) s.kf[q] = c->kf[q];
     s.ds = c->ds;
-    const int ord = k.order == 0 ? 3 : k.order;
-    (void)ord;
     s.sigma = k.sigma;
-    s.kc = c->kc;
     s.nkx = c->nkx;
+    s.correct = (!c->fp32 && s.tab.ndr > 0) ? 1 : 0;
+    s.npiv = c->npiv;
+    s.pivtab = nullptr;
+    if (c->have_piv && k.order >= 1 && k.order <= 3)
+        s.pivtab = (const T*)c->pivtab + ((size_t)((k.order - 1) * 3 + k.blk) * c->nkeys) * c->npiv;
     // diagonal of G (Gmatrix_2dcomp_mod.f90:394): c0 + ds*Loa*l(l+1)/(2 kappa)
     s.dcoef = c->ds * c->p.loa / (2.0 * c->p.kappa[k.blk]);
     return L;
@@ -739,9 +780,9 @@ template <typename T> static int one_step_impl(wlc_ctx* c, StepKind k, const dou
     CK(cudaMemcpyAsync(c->stage, pr, sizeof(double) * sl, cudaMemcpyHostToDevice, c->st));
     launch_to_internal<T>(c->stage, (T*)c->work, c->M, c->nr, c->st);
     c->launches++;
-    StepKind k0 = k;
-    k0.order = 0;
-    StepLaunch<T> L = make_launch<T>(c, k0, (const T*)c->work, nullptr, nullptr, (T*)c->work);
+    // the solve uses the BDF order of G_index; the right-hand side is given
+    StepLaunch<T> L = make_launch<T>(c, k, (const T*)c->work, nullptr, nullptr, (T*)c->work);
+    L.step.order = 0;
     int rc = run_step<T>(c, L, lit_c0(k.order, c->real4), 0);
     if (rc) return rc;
     launch_to_reference<T>((const T*)c->work, c->stage, c->M, c->nr, c->st);

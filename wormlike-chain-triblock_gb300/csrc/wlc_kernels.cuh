@@ -42,24 +42,29 @@ template <typename T> struct StepArgs {
     T minv;             // 1/N^3
 };
 
-// Per-context constant data of the factorised solve (device pointers;
-// values in the compute type T).
+// Per-context constant data of the factorised solve (device pointers).
+// Values are in the compute type T; the *f copies in FP32 serve the
+// first-order correction, which runs in FP32 inside the FP64 path.
 template <typename T> struct SolveTablesT {
     int L, M;
     int npairs;              // (l, m>0) pairs
     const int16_t* pairs;    // [npairs][3]: index of (l, m), index of (l, -m), m
+    int nnz;                 // entries of Xp (= entries of Xm)
     const int* xp_ptr;       // CSR of Xp over output rows
     const int16_t* xp_col;
     const T* xp_val;
+    const float* xp_valf;
     const int* xm_ptr;       // CSR of Xm = Xp^T
     const int16_t* xm_col;
     const T* xm_val;
+    const float* xm_valf;
     const T* zoff;           // [M] Rz coupling (l, m) -> (l+1, m)
+    const float* zofff;
     int ndr;                 // correction entries (0: none)
     const int* dr_ptr;       // CSR over rows
     const int16_t* dr_col;
     const int8_t* dr_axis;   // 0 x, 1 y, 2 z
-    const T* dr_val;
+    const float* dr_valf;
 };
 
 template <typename T> struct SolveArgs {
@@ -72,8 +77,62 @@ template <typename T> struct SolveArgs {
     double c0;          // BDF diagonal
     double dcoef;       // ds * Loa / (2 kappa)
     int sigma;          // +1 forward, -1 backward
-    int kc;             // k chunk (columns of the temp buffers)
     int nkx;
+    int correct;        // apply the FP32 first-order correction (tab.ndr > 0)
+    const T* pivtab;    // [key][npiv] inverse tridiagonal pivots of this
+                        // (order, block), key = ix^2+iy^2+iz^2; null: on the fly
+    int npiv;           // (L+1)(L+2)/2
 };
+
+// Shared-memory carve-up of the solve kernel (bytes, 16-aligned), shared by
+// the host launcher and the kernel.
+struct SolveSmem {
+    size_t col, tw, csa, csaf, wtmp, wrf, wtmf, wcsb, wcsbf;
+    size_t pairs, xp_ptr, xp_col, xp_val, xp_valf, xm_ptr, xm_col, xm_val, xm_valf, zoff, zofff;
+    size_t dr_ptr, dr_col, dr_axis, dr_valf;
+    size_t total;
+};
+
+__host__ __device__ inline size_t al16(size_t v) { return (v + 15) & ~(size_t)15; }
+
+__host__ __device__ inline SolveSmem solve_smem(int N, int M, int L, int nw, int npairs, int nnz, int ndr, int tsize,
+                                               int correct) {
+    SolveSmem s;
+    size_t o = 0;
+    const size_t cs = 2 * (size_t)tsize;
+    auto take = [&](size_t bytes) {
+        const size_t at = o;
+        o = al16(o + bytes);
+        return at;
+    };
+    s.col = take(cs * (size_t)M * (N + 1));
+    s.tw = take(cs * N);
+    s.csa = take((size_t)tsize * 2 * (L + 1));
+    s.csaf = take(correct ? 4 * 2 * (size_t)(L + 1) : 0);
+    s.wtmp = take(cs * (size_t)M * nw);
+    s.wrf = take(correct ? 8 * (size_t)M * nw : 0);
+    s.wtmf = take(correct ? 8 * (size_t)M * nw : 0);
+    s.wcsb = take((size_t)tsize * (2 * (L + 1) + 1) * N);     // per kz: cos/sin(m beta), then t
+    s.wcsbf = take(correct ? 4 * (size_t)(2 * (L + 1) + 2) * N : 0);  // FP32 copy, t and kz
+    s.pairs = take(2 * 3 * (size_t)npairs);
+    s.xp_ptr = take(4 * (size_t)(M + 1));
+    s.xp_col = take(2 * (size_t)nnz);
+    s.xp_val = take((size_t)tsize * nnz);
+    s.xp_valf = take(correct ? 4 * (size_t)nnz : 0);
+    s.xm_ptr = take(4 * (size_t)(M + 1));
+    s.xm_col = take(2 * (size_t)nnz);
+    s.xm_val = take((size_t)tsize * nnz);
+    s.xm_valf = take(correct ? 4 * (size_t)nnz : 0);
+    s.zoff = take((size_t)tsize * M);
+    s.zofff = take(correct ? 4 * (size_t)M : 0);
+    s.dr_ptr = take(correct ? 4 * (size_t)(M + 1) : 0);
+    s.dr_col = take(correct ? 2 * (size_t)ndr : 0);
+    s.dr_axis = take(correct ? (size_t)ndr : 0);
+    s.dr_valf = take(correct ? 4 * (size_t)ndr : 0);
+    s.total = o;
+    return s;
+}
+
+constexpr int kSolveWarpsMax = 16;  // warps per CTA of the solve kernel (fewer if shared memory is short)
 
 }  // namespace wlc

@@ -50,7 +50,6 @@ struct DevState {
     wlc::SolveTablesT<double> tab{};
     double2* twg = nullptr;
     double2* phat = nullptr;
-    int kc = 0;
 };
 
 std::mutex g_mu;
@@ -113,22 +112,27 @@ TableImage make_image(const wlc::BasisTables& t, unsigned char* base) {
     }
     auto& img = im.bytes;
     wlc::SolveTablesT<double>& s = im.tab;
+    auto f32 = [](const std::vector<double>& v) { return std::vector<float>(v.begin(), v.end()); };
     s.L = t.L;
     s.M = t.M;
     s.npairs = (int)pairs.size() / 3;
+    s.nnz = (int)t.xp_val.size();
     s.pairs = reinterpret_cast<const int16_t*>(base + put(img, pairs));
     s.xp_ptr = reinterpret_cast<const int*>(base + put(img, t.xp_ptr));
     s.xp_col = reinterpret_cast<const int16_t*>(base + put(img, i16(t.xp_col)));
     s.xp_val = reinterpret_cast<const double*>(base + put(img, t.xp_val));
+    s.xp_valf = reinterpret_cast<const float*>(base + put(img, f32(t.xp_val)));
     s.xm_ptr = reinterpret_cast<const int*>(base + put(img, t.xm_ptr));
     s.xm_col = reinterpret_cast<const int16_t*>(base + put(img, i16(t.xm_col)));
     s.xm_val = reinterpret_cast<const double*>(base + put(img, t.xm_val));
+    s.xm_valf = reinterpret_cast<const float*>(base + put(img, f32(t.xm_val)));
     s.zoff = reinterpret_cast<const double*>(base + put(img, t.zoff));
+    s.zofff = reinterpret_cast<const float*>(base + put(img, f32(t.zoff)));
     s.ndr = (int)dval.size();
     s.dr_ptr = reinterpret_cast<const int*>(base + put(img, dptr));
     s.dr_col = reinterpret_cast<const int16_t*>(base + put(img, dcol));
     s.dr_axis = reinterpret_cast<const int8_t*>(base + put(img, dax));
-    s.dr_val = reinterpret_cast<const double*>(base + put(img, dval));
+    s.dr_valf = reinterpret_cast<const float*>(base + put(img, f32(dval)));
     img.resize(align256(img.size()));
     return im;
 }
@@ -194,14 +198,14 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
                       N, L, need, kScratchBytes);
         return fail(errbuf, errlen, WLC_E_UNSUPPORTED, buf);
     }
-    int kc = 0;
-    for (int c : {16, 8, 4, 2, 1})
-        if (c <= N && smem_solve<double>(N, M, L, c) <= 227 * 1024) {
-            kc = c;
-            break;
-        }
-    if (kc == 0 || smem_xy<double>(N) > 227 * 1024)
-        return fail(errbuf, errlen, WLC_E_UNSUPPORTED, "one coefficient column does not fit in shared memory");
+    {
+        const BasisTables& t = it->second;
+        const int ndr = (int)(t.dR[0].size() + t.dR[1].size() + t.dR[2].size());
+        const size_t ssv =
+            solve_smem(N, M, L, 8, L * (L + 1) / 2, (int)t.xp_val.size(), ndr, 8, ndr > 0 ? 1 : 0).total;
+        if (ssv > 227 * 1024 || smem_xy<double>(N) > 227 * 1024)
+            return fail(errbuf, errlen, WLC_E_UNSUPPORTED, "one coefficient column does not fit in shared memory");
+    }
     if (ds.L != L || ds.real4 != real4 || ds.N != N) {
         std::vector<double2> tw(N);
         for (int j = 0; j < N; ++j) {
@@ -247,8 +251,10 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
     s.c0 = lit_c0(order, real4);
     s.dcoef = s.ds * p->loa / (2.0 * p->kappa[blk]);
     s.sigma = sigma;
-    s.kc = kc;
     s.nkx = N / 2 + 1;
+    s.correct = ds.tab.ndr > 0 ? 1 : 0;
+    s.pivtab = nullptr;  // pivots computed in the kernel: no table to hold
+    s.npiv = (L + 1) * (L + 2) / 2;
     cudaError_t e = launch_step<double>(N, Lh, st);
     if (e != cudaSuccess) return fail(errbuf, errlen, WLC_E_CUDA, std::string("launch: ") + cudaGetErrorString(e));
     return WLC_OK;

@@ -19,7 +19,11 @@ template <typename T> struct StepLaunch {
 template <typename T> cudaError_t launch_step(int N, const StepLaunch<T>& s, cudaStream_t st);
 template <typename T> cudaError_t launch_rhs_only(int N, const StepArgs<T>& a, T* out, cudaStream_t st);
 template <typename T> size_t smem_xy(int N);
-template <typename T> size_t smem_solve(int N, int M, int L, int kc);
+template <typename T> cudaError_t launch_solve(int N, const SolveArgs<T>& a, cudaStream_t st);
+template <typename T> size_t solve_smem_bytes(const SolveArgs<T>& a);
+template <typename T>
+cudaError_t launch_pivot_table(T* out, int nkeys, int L, double c0, double dcoef, double ds, double kf, const T* zoff,
+                               cudaStream_t st);
 
 inline bool supported_n(int n) {
     switch (n) {
