@@ -282,7 +282,7 @@ template <typename T> static int alloc_fields(wlc_ctx* c) {
     c->qb = pt;
     if ((rc = dalloc(c, &pc, sizeof(C) * (size_t)c->nk * c->M))) return rc;
     c->phat = pc;
-    if ((rc = dalloc(c, &pt, sizeof(T) * 9 * (size_t)c->nr))) return rc;
+    if ((rc = dalloc(c, &pt, sizeof(T) * 12 * (size_t)c->nr))) return rc;  // cf[3][3][nr] + dsw[3][nr]
     c->cf = pt;
     if ((rc = dalloc(c, &pt, sizeof(T) * sl))) return rc;
     c->work = pt;
@@ -487,6 +487,8 @@ static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h
     a.h3 = h3;
     a.wb = c->w + (size_t)k.blk * nr;
     a.cf = (const T*)c->cf + (size_t)k.blk * 3 * nr;
+    a.dsw = (const T*)c->cf + (size_t)(9 + k.blk) * nr;
+    a.third = (T)lit_third(c->real4);
     a.msterm = nullptr;
     a.order = k.order;
     a.ds = (T)c->ds;

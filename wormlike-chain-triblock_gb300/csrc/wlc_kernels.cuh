@@ -31,6 +31,8 @@ template <typename T> struct StepArgs {
     const T* h3;
     const double* wb;   // block field [nr] (orders 1, 2)
     const T* cf;        // order-3 coefficient planes [3][nr]
+    const T* dsw;       // ds * w of the block [nr] (FP32 staged path)
+    T third;            // 1/3 of the BDF3 history (literal semantics)
     const T* msterm;    // optional ds*Theta*h term [M][nr] (Maier-Saupe) or null
     int order;          // 0: h1 is the right-hand side itself; 1..3 BDF order
     T ds;

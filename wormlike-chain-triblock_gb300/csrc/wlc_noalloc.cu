@@ -234,6 +234,8 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
     a.h3 = nullptr;
     a.wb = nullptr;
     a.cf = nullptr;
+    a.dsw = nullptr;
+    a.third = lit_third(real4);
     a.msterm = nullptr;
     a.order = 0;  // the right-hand side is given
     a.ds = 1.0 / (double)p->nmax;

@@ -35,17 +35,61 @@ __device__ __forceinline__ T rhs_value(const StepArgs<T>& a, size_t off, size_t 
     return v;
 }
 
+// ------------------------------------------------------- async copies
+__device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int n> __device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(n) : "memory");
+}
+
+// The half-spectrum planes of a CTA are kept z-fastest, out[(ky*NKX + kx)*Z + zz],
+// so that the Z values of one (col, i) run in phat move as one 32-byte chunk.
+
+// x-FFT of packed row pairs, split into two half spectra, y-FFT; plane zz of out
+template <typename T, int N, int Z>
+__device__ __forceinline__ void fwd_xy_plane(typename cvec<T>::t* zb, typename cvec<T>::t* out, int zz,
+                                             const typename cvec<T>::t* tw) {
+    using C = typename cvec<T>::t;
+    constexpr int NKX = N / 2 + 1;
+    fft_nat2perm<N, -1>(zb, N / 2, 1, N, tw);
+    for (int e = threadIdx.x; e < (N / 2) * NKX; e += blockDim.x) {
+        const int p = e / NKX, k = e % NKX;
+        const C zk = zb[p * N + perm_pos<N>(k)];
+        const C zm = zb[p * N + perm_pos<N>((N - k) % N)];
+        out[((2 * p) * NKX + k) * Z + zz] = cmk<C>((T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y - zm.y));
+        out[((2 * p + 1) * NKX + k) * Z + zz] = cmk<C>((T)0.5 * (zk.y + zm.y), (T)0.5 * (zm.x - zk.x));
+    }
+    __syncthreads();
+    fft_nat2perm<N, -1>(out + zz, NKX, NKX * Z, Z, tw);
+}
+
+template <typename T, int N, int Z>
+__device__ __forceinline__ void store_phat(const StepArgs<T>& a, const typename cvec<T>::t* out, int i, int z0) {
+    using C = typename cvec<T>::t;
+    constexpr int NKX = N / 2 + 1;
+    for (int e = threadIdx.x; e < N * NKX; e += blockDim.x) {
+        const int ky = e / NKX, kx = e % NKX;
+        const size_t colid = (size_t)ky * NKX + kx;
+        C* dst = a.phat + (colid * a.M + i) * N + z0;
+        const C* src = out + (size_t)(perm_pos<N>(ky) * NKX + kx) * Z;
+#pragma unroll
+        for (int zz = 0; zz < Z; ++zz) dst[zz] = src[zz];
+    }
+}
+
 // ---------------------------------------------------------------- pass A
 template <typename T, int N>
 __global__ void __launch_bounds__(256) rhs_fft_xy(StepArgs<T> a) {
     using C = typename cvec<T>::t;
     constexpr int Z = zg_planes(N, sizeof(T));
-    constexpr int NKX = N / 2 + 1;
     constexpr int NR = N * N * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* zb = tw + N;              // (N/2) x N packed row pairs
-    C* out = zb + (N / 2) * N;   // Z x N x NKX half spectra
+    C* out = zb + (N / 2) * N;   // N x NKX x Z half spectra
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
@@ -59,27 +103,90 @@ __global__ void __launch_bounds__(256) rhs_fft_xy(StepArgs<T> a) {
             zb[e] = cmk<C>(va, vb);
         }
         __syncthreads();
-        fft_nat2perm<N, -1>(zb, N / 2, 1, N, tw);
-        C* o = out + (size_t)zz * N * NKX;
-        // split the transform of (row 2p) + i (row 2p+1) into two half spectra
-        for (int e = threadIdx.x; e < (N / 2) * NKX; e += blockDim.x) {
-            const int p = e / NKX, k = e % NKX;
-            const C zk = zb[p * N + perm_pos<N>(k)];
-            const C zm = zb[p * N + perm_pos<N>((N - k) % N)];
-            o[(2 * p) * NKX + k] = cmk<C>((T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y - zm.y));
-            o[(2 * p + 1) * NKX + k] = cmk<C>((T)0.5 * (zk.y + zm.y), (T)0.5 * (zm.x - zk.x));
+        fwd_xy_plane<T, N, Z>(zb, out, zz, tw);
+    }
+    store_phat<T, N, Z>(a, out, i, z0);
+}
+
+// FP32 pass A with the history planes staged by cp.async, double-buffered
+// across the CTA's z planes (plane zz+1 in flight while zz is transformed).
+template <int N> struct StagedA {
+    static constexpr int Z = zg_planes(N, 4);
+    static constexpr size_t P = (size_t)N * N;
+    static constexpr size_t bytes = 8 * ((size_t)N + (N / 2) * (size_t)N + (size_t)Z * N * (N / 2 + 1)) + 2 * 4 * P * 4;
+    static constexpr bool fits = bytes <= 220 * 1024;
+};
+
+__device__ __forceinline__ float rhs_staged(const float* st, int order, size_t P, size_t idx, float third) {
+    const float q1 = st[idx];
+    if (order == 0) return q1;
+    if (order == 1) return (1.0f - st[P + idx]) * q1;
+    if (order == 2) {
+        const float q2 = st[P + idx], dw = st[2 * P + idx];
+        return 2.0f * q1 - 0.5f * q2 - dw * (2.0f * q1 - q2);
+    }
+    const float q2 = st[P + idx], q3 = st[2 * P + idx], dw = st[3 * P + idx];
+    const float c1 = 3.0f - 3.0f * dw, c2 = -1.5f + 3.0f * dw, c3 = third - dw;
+    return fmaf(c3, q3, fmaf(c2, q2, c1 * q1));
+}
+
+template <int N>
+__global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a) {
+    using C = float2;
+    constexpr int Z = StagedA<N>::Z;
+    constexpr int NKX = N / 2 + 1;
+    constexpr int NR = N * N * N;
+    constexpr size_t P = StagedA<N>::P;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* tw = reinterpret_cast<C*>(smem_raw);
+    C* zb = tw + N;
+    C* out = zb + (N / 2) * N;
+    float* stage = reinterpret_cast<float*>(out + (size_t)Z * N * NKX);  // [2][4][P]
+    const int i = blockIdx.y;
+    const int z0 = blockIdx.x * Z;
+    const int order = a.order;
+    const float* src[4];
+    int ns = 0;
+    src[ns++] = a.h1 + (size_t)i * NR;
+    if (order >= 2) src[ns++] = a.h2 + (size_t)i * NR;
+    if (order >= 3) src[ns++] = a.h3 + (size_t)i * NR;
+    if (order >= 1) src[ns++] = a.dsw;
+    auto issue = [&](int zz, int buf) {
+        const size_t zoff = (size_t)(z0 + zz) * P;
+        for (int q = 0; q < ns; ++q) {
+            const float* g = src[q] + zoff;
+            float* d = stage + ((size_t)buf * 4 + q) * P;
+            for (size_t e = (size_t)threadIdx.x * 4; e < P; e += (size_t)blockDim.x * 4) cp_async16(d + e, g + e);
+        }
+        cp_async_commit();
+    };
+    for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
+    issue(0, 0);
+    for (int zz = 0; zz < Z; ++zz) {
+        if (zz + 1 < Z) {
+            issue(zz + 1, (zz + 1) & 1);
+            cp_async_wait<1>();
+        } else {
+            cp_async_wait<0>();
         }
         __syncthreads();
-        fft_nat2perm<N, -1>(o, NKX, NKX, 1, tw);
+        const float* st = stage + (size_t)(zz & 1) * 4 * P;
+        const size_t zoff = (size_t)(z0 + zz) * P;
+        for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
+            const int p = e / N, x = e % N;
+            const size_t ia = (size_t)(2 * p) * N + x, ib = ia + N;
+            float va = rhs_staged(st, order, P, ia, a.third);
+            float vb = rhs_staged(st, order, P, ib, a.third);
+            if (a.msterm) {
+                va += a.msterm[(size_t)i * NR + zoff + ia];
+                vb += a.msterm[(size_t)i * NR + zoff + ib];
+            }
+            zb[e] = make_float2(va, vb);
+        }
+        __syncthreads();
+        fwd_xy_plane<float, N, Z>(zb, out, zz, tw);
     }
-    for (int e = threadIdx.x; e < N * NKX; e += blockDim.x) {
-        const int ky = e / NKX, kx = e % NKX;
-        const size_t colid = (size_t)ky * NKX + kx;
-        C* dst = a.phat + (colid * a.M + i) * N + z0;
-        const int pos = perm_pos<N>(ky) * NKX + kx;
-#pragma unroll
-        for (int zz = 0; zz < Z; ++zz) dst[zz] = out[(size_t)zz * N * NKX + pos];
-    }
+    store_phat<float, N, Z>(a, out, i, z0);
 }
 
 // ---------------------------------------------------------------- pass C
@@ -96,32 +203,37 @@ __global__ void __launch_bounds__(256) ifft_xy(StepArgs<T> a) {
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
-    for (int e = threadIdx.x; e < N * NKX; e += blockDim.x) {
-        const C* src = a.phat + ((size_t)e * a.M + i) * N + z0;
-#pragma unroll
-        for (int zz = 0; zz < Z; ++zz) out[(size_t)zz * N * NKX + e] = src[zz];
+    // all loads issued up front: one Z-run (Z * sizeof(C) bytes) per (ky, kx)
+    constexpr int CH = (Z * (int)sizeof(C)) / 16;  // 16-byte chunks per run
+    static_assert((Z * sizeof(C)) % 16 == 0, "phat runs must be whole 16-byte chunks");
+    for (int e = threadIdx.x; e < N * NKX * CH; e += blockDim.x) {
+        const int col = e / CH, q = e % CH;
+        const C* src = a.phat + ((size_t)col * a.M + i) * N + z0;
+        cp_async16(reinterpret_cast<unsigned char*>(out + (size_t)col * Z) + 16 * q,
+                   reinterpret_cast<const unsigned char*>(src) + 16 * q);
     }
+    cp_async_commit();
+    cp_async_wait<0>();
     __syncthreads();
     for (int zz = 0; zz < Z; ++zz) {
-        C* o = out + (size_t)zz * N * NKX;
-        fft_nat2perm<N, +1>(o, NKX, NKX, 1, tw);  // along y; row y now at perm_pos(y)
+        fft_nat2perm<N, +1>(out + zz, NKX, NKX * Z, Z, tw);  // along y; row y now at perm_pos(y)
         // Hermitian extension of rows (2p, 2p+1) packed as one complex row;
         // the imaginary parts at kx = 0 and N/2 are discarded (c2r)
         for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
             const int p = e / N, k = e % N;
-            const C* ra = o + perm_pos<N>(2 * p) * NKX;
-            const C* rb = o + perm_pos<N>(2 * p + 1) * NKX;
+            const C* ra = out + (size_t)perm_pos<N>(2 * p) * NKX * Z + zz;
+            const C* rb = out + (size_t)perm_pos<N>(2 * p + 1) * NKX * Z + zz;
             C xa, xb;
             if (k <= N / 2) {
-                xa = ra[k];
-                xb = rb[k];
+                xa = ra[k * Z];
+                xb = rb[k * Z];
                 if (k == 0 || k == N / 2) {
                     xa.y = (T)0;
                     xb.y = (T)0;
                 }
             } else {
-                xa = ra[N - k];
-                xb = rb[N - k];
+                xa = ra[(N - k) * Z];
+                xb = rb[(N - k) * Z];
                 xa.y = -xa.y;
                 xb.y = -xb.y;
             }
@@ -161,11 +273,19 @@ template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s,
     if (!attr_done) {
         cudaFuncSetAttribute(rhs_fft_xy<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
         cudaFuncSetAttribute(ifft_xy<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
+            cudaFuncSetAttribute(rhs_fft_xy_staged<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)StagedA<N>::bytes);
         attr_done = true;
     }
     const dim3 gxy(N / Z, s.step.M);
     if (s.events) cudaEventRecord(s.events[0], st);
-    if (s.do_a) rhs_fft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step);
+    if (s.do_a) {
+        if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
+            rhs_fft_xy_staged<N><<<gxy, 512, StagedA<N>::bytes, st>>>(s.step);
+        else
+            rhs_fft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step);
+    }
     if (s.events) cudaEventRecord(s.events[1], st);
     if (s.do_b) launch_solve<T>(N, s.solve, st);
     if (s.events) cudaEventRecord(s.events[2], st);
