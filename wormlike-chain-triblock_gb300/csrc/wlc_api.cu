@@ -326,9 +326,8 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
         int npairs = c->L * (c->L + 1) / 2, ndr = 0;
         for (int a = 0; a < 3; ++a) ndr += (int)c->tab.dR[a].size();
         const bool corr = !c->fp32 && ndr > 0;
-        const size_t ssv = solve_smem(c->N, c->M, c->L, 8, npairs, (int)c->tab.xp_val.size(), ndr,
-                                      c->fp32 ? 4 : 8, corr ? 1 : 0)
-                               .total;
+        (void)npairs;
+        const size_t ssv = solve_smem(c->N, c->M, c->L, ndr, c->fp32 ? 4 : 8, corr ? 1 : 0).total;
         if (ssv > 227 * 1024 || sxy > 227 * 1024)
             return set_err(c, WLC_E_UNSUPPORTED, "one coefficient column (M x N) does not fit in shared memory for "
                                                  "this (N, L, precision)");

@@ -89,16 +89,13 @@ template <typename T> struct SolveArgs {
 // Shared-memory carve-up of the solve kernel (bytes, 16-aligned), shared by
 // the host launcher and the kernel.
 struct SolveSmem {
-    size_t col, tw, csa, csaf, wtmp, wrf, wtmf, wcsb, wcsbf;
-    size_t pairs, xp_ptr, xp_col, xp_val, xp_valf, xm_ptr, xm_col, xm_val, xm_valf, zoff, zofff;
-    size_t dr_ptr, dr_col, dr_axis, dr_valf;
+    size_t col, tw, csa, csaf, zoff, zofff, dr_ptr, dr_col, dr_axis, dr_valf, corr, masks;
     size_t total;
 };
 
 __host__ __device__ inline size_t al16(size_t v) { return (v + 15) & ~(size_t)15; }
 
-__host__ __device__ inline SolveSmem solve_smem(int N, int M, int L, int nw, int npairs, int nnz, int ndr, int tsize,
-                                               int correct) {
+__host__ __device__ inline SolveSmem solve_smem(int N, int M, int L, int ndr, int tsize, int correct) {
     SolveSmem s;
     size_t o = 0;
     const size_t cs = 2 * (size_t)tsize;
@@ -110,31 +107,19 @@ __host__ __device__ inline SolveSmem solve_smem(int N, int M, int L, int nw, int
     s.col = take(cs * (size_t)M * (N + 1));
     s.tw = take(cs * N);
     s.csa = take((size_t)tsize * 2 * (L + 1));
-    s.csaf = take(correct ? 4 * 2 * (size_t)(L + 1) : 0);
-    s.wtmp = take(cs * (size_t)M * nw);
-    s.wrf = take(correct ? 8 * (size_t)M * nw : 0);
-    s.wtmf = take(correct ? 8 * (size_t)M * nw : 0);
-    s.wcsb = take((size_t)tsize * (2 * (L + 1) + 1) * N);     // per kz: cos/sin(m beta), then t
-    s.wcsbf = take(correct ? 4 * (size_t)(2 * (L + 1) + 2) * N : 0);  // FP32 copy, t and kz
-    s.pairs = take(2 * 3 * (size_t)npairs);
-    s.xp_ptr = take(4 * (size_t)(M + 1));
-    s.xp_col = take(2 * (size_t)nnz);
-    s.xp_val = take((size_t)tsize * nnz);
-    s.xp_valf = take(correct ? 4 * (size_t)nnz : 0);
-    s.xm_ptr = take(4 * (size_t)(M + 1));
-    s.xm_col = take(2 * (size_t)nnz);
-    s.xm_val = take((size_t)tsize * nnz);
-    s.xm_valf = take(correct ? 4 * (size_t)nnz : 0);
+    s.csaf = take(4 * 2 * (size_t)(L + 1));
     s.zoff = take((size_t)tsize * M);
     s.zofff = take(correct ? 4 * (size_t)M : 0);
     s.dr_ptr = take(correct ? 4 * (size_t)(M + 1) : 0);
     s.dr_col = take(correct ? 2 * (size_t)ndr : 0);
     s.dr_axis = take(correct ? (size_t)ndr : 0);
     s.dr_valf = take(correct ? 4 * (size_t)ndr : 0);
+    s.corr = take(correct ? 8 * (size_t)M * N : 0);  // FP32 correction vectors [i][kz]
+    s.masks = take(4 * 2 * 32);                      // work split of the solve phase
     s.total = o;
     return s;
 }
 
-constexpr int kSolveWarpsMax = 16;  // warps per CTA of the solve kernel (fewer if shared memory is short)
+constexpr int kSolveThreads = 256;  // threads per CTA of the solve kernel (kz x parts in the solve phase)
 
 }  // namespace wlc

@@ -202,7 +202,7 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
         const BasisTables& t = it->second;
         const int ndr = (int)(t.dR[0].size() + t.dR[1].size() + t.dR[2].size());
         const size_t ssv =
-            solve_smem(N, M, L, 8, L * (L + 1) / 2, (int)t.xp_val.size(), ndr, 8, ndr > 0 ? 1 : 0).total;
+            solve_smem(N, M, L, ndr, 8, ndr > 0 ? 1 : 0).total;
         if (ssv > 227 * 1024 || smem_xy<double>(N) > 227 * 1024)
             return fail(errbuf, errlen, WLC_E_UNSUPPORTED, "one coefficient column does not fit in shared memory");
     }

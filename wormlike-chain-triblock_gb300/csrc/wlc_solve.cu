@@ -5,134 +5,162 @@
 //
 // Factorised solve (see wlc_host.cpp): G^-1 = D T^-1 D^T with
 // D = Dz(alpha) Xm Dz(beta) Xp and T = A + i sigma ds |k| Rz, one
-// tridiagonal system per m.  One warp owns one kz at a time and runs the
-// whole solve warp-synchronously (no CTA barrier); the column lives in
-// shared memory with line stride N+1 so that the per-k strided accesses are
-// bank-conflict free.  Operator tables are staged in shared memory.
-// Tridiagonal pivots come from a per-(order, block) table keyed by
-// ix^2+iy^2+iz^2 when the grid spacing is isotropic.
+// tridiagonal system per m.  One thread owns one kz and runs the whole
+// solve: the rotations block by block in registers with the generated
+// constant codelets (wlc_rot_gen.cuh), the tridiagonal sweeps through its
+// slot of the shared column (line stride N+1, conflict free).  Tridiagonal
+// pivots come from a per-(order, block) table keyed by ix^2+iy^2+iz^2 when
+// the grid spacing is isotropic.
 #include <cstdio>
 
 #include "wlc_kernels.cuh"
+#include "wlc_rot_gen.cuh"
 #include "wlc_step.h"
 
 namespace wlc {
 
 __device__ __forceinline__ int fold_n(int i, int n) { return i <= n / 2 ? i : i - n; }
 
-// shared-memory views of the tables for one solve type TS
-template <typename TS> struct WTab {
-    int L, M, npairs;
-    const int16_t* pairs;
-    const int* xp_ptr;
-    const int16_t* xp_col;
-    const TS* xp_val;
-    const int* xm_ptr;
-    const int16_t* xm_col;
-    const TS* xm_val;
-    const TS* zoff;
-};
+// ---------------------------------------------------------------------
+// Per-wavevector solve, one thread per kz.  The thread's coefficient
+// vector is column p of the shared column buffer (element i at v[i*vs]);
+// lanes of a warp own consecutive p, so every access is bank-conflict free.
+// Rotations work block by block (degree l) in registers with the
+// generated constant codelets; the tridiagonal sweeps run through the
+// shared column.
 
-template <typename TS, typename CS>
-__device__ __forceinline__ void w_dz(CS* v, int vs, const TS* cs, int sgn, const WTab<TS>& t, int lane) {
-    for (int q = lane; q < t.npairs; q += 32) {
-        const int ic = t.pairs[3 * q], is = t.pairs[3 * q + 1], m = t.pairs[3 * q + 2];
-        const TS cm = cs[2 * m], sm = sgn > 0 ? cs[2 * m + 1] : -cs[2 * m + 1];
-        const CS x = v[ic * vs], y = v[is * vs];
-        v[ic * vs] = cmk<CS>(cm * x.x - sm * y.x, cm * x.y - sm * y.y);
-        v[is * vs] = cmk<CS>(sm * x.x + cm * y.x, sm * x.y + cm * y.y);
+// Dz(sgn * gamma) on the (m, -m) pairs of register block a (index m+l)
+template <int l, typename T, typename C>
+__device__ __forceinline__ void dz_block(C* a, const T* cs, int sgn) {
+#pragma unroll
+    for (int m = 1; m <= l; ++m) {
+        const T cm = cs[2 * m], sm = sgn > 0 ? cs[2 * m + 1] : -cs[2 * m + 1];
+        const C x = a[l + m], y = a[l - m];
+        a[l + m] = cmk<C>(cm * x.x - sm * y.x, cm * x.y - sm * y.y);
+        a[l - m] = cmk<C>(sm * x.x + cm * y.x, sm * x.y + cm * y.y);
     }
 }
 
-template <typename TS, typename CS>
-__device__ __forceinline__ void w_csr(const int* ptr, const int16_t* col, const TS* val, const CS* in, int is, CS* out,
-                                      int os, int M, int lane) {
-    for (int i = lane; i < M; i += 32) {
-        TS ax = 0, ay = 0;
-        const int e1 = ptr[i + 1];
-        for (int e = ptr[i]; e < e1; ++e) {
-            const TS g = val[e];
-            const CS x = in[col[e] * is];
-            ax = fma(g, x.x, ax);
-            ay = fma(g, x.y, ay);
+// D^T on block l: Xm Dz(-beta) Xp Dz(-alpha)
+template <int l, typename T, typename C>
+__device__ __forceinline__ void rot_in_block(C* v, int vs, const T* csa, const T* csb) {
+    constexpr int n = 2 * l + 1;
+    C a[n], b[n];
+#pragma unroll
+    for (int j = 0; j < n; ++j) a[j] = v[(l * l + j) * vs];
+    dz_block<l, T, C>(a, csa, -1);
+    XRot<l>::template p<T, C>(a, b);
+    dz_block<l, T, C>(b, csb, -1);
+    XRot<l>::template m<T, C>(b, a);
+#pragma unroll
+    for (int j = 0; j < n; ++j) v[(l * l + j) * vs] = a[j];
+}
+
+// D on block l: Dz(alpha) Xm Dz(beta) Xp
+template <int l, typename T, typename C>
+__device__ __forceinline__ void rot_out_block(C* v, int vs, const T* csa, const T* csb) {
+    constexpr int n = 2 * l + 1;
+    C a[n], b[n];
+#pragma unroll
+    for (int j = 0; j < n; ++j) a[j] = v[(l * l + j) * vs];
+    XRot<l>::template p<T, C>(a, b);
+    dz_block<l, T, C>(b, csb, +1);
+    XRot<l>::template m<T, C>(b, a);
+    dz_block<l, T, C>(a, csa, +1);
+#pragma unroll
+    for (int j = 0; j < n; ++j) v[(l * l + j) * vs] = a[j];
+}
+
+// D^T (in = 1) or D (in = 0) on the degree blocks l set in lmask;
+// cos/sin(m beta) by recurrence from (cb, sb).  Compiled once per precision.
+template <typename T>
+__device__ __noinline__ void rot_all(typename cvec<T>::t* v, int vs, int L, const T* csa, T cb, T sb, int in,
+                                     unsigned lmask) {
+    using C = typename cvec<T>::t;
+    T csb[2 * (kRotLmax + 1)];
+    {
+        T cm = (T)1, sm2 = (T)0;
+#pragma unroll
+        for (int m = 0; m <= kRotLmax; ++m) {
+            csb[2 * m] = cm;
+            csb[2 * m + 1] = sm2;
+            const T cn = cm * cb - sm2 * sb, sn = sm2 * cb + cm * sb;
+            cm = cn;
+            sm2 = sn;
         }
-        out[i * os] = cmk<CS>(ax, ay);
+    }
+#pragma unroll 1
+    for (int l = 0; l <= L; ++l) {
+        if (!((lmask >> l) & 1u)) continue;
+        switch (l) {
+#define WLC_ROT(q)                                          \
+    case q:                                                 \
+        if (in)                                             \
+            rot_in_block<q, T, C>(v, vs, csa, csb);         \
+        else                                                \
+            rot_out_block<q, T, C>(v, vs, csa, csb);        \
+        break;
+            WLC_ROT(0) WLC_ROT(1) WLC_ROT(2) WLC_ROT(3) WLC_ROT(4) WLC_ROT(5) WLC_ROT(6)
+            WLC_ROT(7) WLC_ROT(8) WLC_ROT(9) WLC_ROT(10) WLC_ROT(11) WLC_ROT(12)
+#undef WLC_ROT
+            default:
+                break;
+        }
     }
 }
 
-// Both systems +m and -m of one m share their real pivots d_j:
+// Tridiagonal systems of one m (both +m and -m share the real pivots):
 // d_0 = A_m, d_j = A_l + e^2/d_{j-1}, e = t z_{l-1}; forward
 // y_l = b_l - i (e/d_{j-1}) y_{l-1}; back x_l = (y_l - i t z_l x_{l+1})/d_l.
-template <typename TS, typename CS>
-__device__ __forceinline__ void w_tridiag(CS* v, int vs, TS t, TS c0, TS dcoef, const WTab<TS>& tb, const TS* pivrow,
-                                          int lane) {
-    const int L = tb.L;
-    for (int m = lane; m <= L; m += 32) {
+template <typename T>
+__device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, T t, T c0, T dcoef, const T* zoff,
+                                         const T* pivrow, unsigned mmask) {
+    using C = typename cvec<T>::t;
+#pragma unroll 1
+    for (int m = 0; m <= L; ++m) {
+        if (!((mmask >> m) & 1u)) continue;
         const int n = L - m + 1;
-        TS dinv[16];
+        T dinv[16];
         if (pivrow) {
-            const TS* pr = pivrow + m * (L + 1) - (m * (m - 1)) / 2;
+            const T* pr = pivrow + m * (L + 1) - (m * (m - 1)) / 2;
             for (int j = 0; j < n; ++j) dinv[j] = pr[j];
         } else {
-            TS d = c0 + dcoef * (TS)(m * (m + 1));
-            dinv[0] = (TS)1 / d;
+            T d = c0 + dcoef * (T)(m * (m + 1));
+            dinv[0] = (T)1 / d;
             for (int j = 1; j < n; ++j) {
                 const int l = m + j;
-                const TS e = t * tb.zoff[(l - 1) * (l - 1) + (l - 1) + m];
-                d = (c0 + dcoef * (TS)(l * (l + 1))) + e * (e * dinv[j - 1]);
-                dinv[j] = (TS)1 / d;
+                const T e = t * zoff[(l - 1) * (l - 1) + (l - 1) + m];
+                d = (c0 + dcoef * (T)(l * (l + 1))) + e * (e * dinv[j - 1]);
+                dinv[j] = (T)1 / d;
             }
         }
         for (int sgn = 1; sgn >= -1; sgn -= 2) {
             if (sgn < 0 && m == 0) break;
             const int mm = sgn * m;
             int idx = m * m + m + mm;
-            CS yp = v[idx * vs];
+            C yp = v[idx * vs];
             for (int j = 1; j < n; ++j) {
                 const int l = m + j;
                 const int prev = idx;
                 idx = l * l + l + mm;
-                const TS g = t * tb.zoff[prev] * dinv[j - 1];
-                CS y = v[idx * vs];
-                y = cmk<CS>(fma(g, yp.y, y.x), fma(-g, yp.x, y.y));
+                const T g = t * zoff[prev] * dinv[j - 1];
+                C y = v[idx * vs];
+                y = cmk<C>(fma(g, yp.y, y.x), fma(-g, yp.x, y.y));
                 v[idx * vs] = y;
                 yp = y;
             }
-            CS xn = cmk<CS>(yp.x * dinv[n - 1], yp.y * dinv[n - 1]);
+            C xn = cmk<C>(yp.x * dinv[n - 1], yp.y * dinv[n - 1]);
             v[idx * vs] = xn;
             for (int j = n - 2; j >= 0; --j) {
                 const int l = m + j;
                 idx = l * l + l + mm;
-                const TS e = t * tb.zoff[idx];
-                const CS y = v[idx * vs];
-                xn = cmk<CS>(fma(e, xn.y, y.x) * dinv[j], fma(-e, xn.x, y.y) * dinv[j]);
+                const T e = t * zoff[idx];
+                const C y = v[idx * vs];
+                xn = cmk<C>(fma(e, xn.y, y.x) * dinv[j], fma(-e, xn.x, y.y) * dinv[j]);
                 v[idx * vs] = xn;
             }
         }
     }
-}
-
-template <typename TS, typename CS>
-__device__ __forceinline__ void w_cov_solve(CS* v, int vs, CS* tmp, const WTab<TS>& tb, const TS* csa, const TS* csb,
-                                            TS t, TS c0, TS dcoef, const TS* pivrow, int lane) {
-    w_dz<TS, CS>(v, vs, csa, -1, tb, lane);
-    __syncwarp();
-    w_csr<TS, CS>(tb.xp_ptr, tb.xp_col, tb.xp_val, v, vs, tmp, 1, tb.M, lane);
-    __syncwarp();
-    w_dz<TS, CS>(tmp, 1, csb, -1, tb, lane);
-    __syncwarp();
-    w_csr<TS, CS>(tb.xm_ptr, tb.xm_col, tb.xm_val, tmp, 1, v, vs, tb.M, lane);
-    __syncwarp();
-    w_tridiag<TS, CS>(v, vs, t, c0, dcoef, tb, pivrow, lane);
-    __syncwarp();
-    w_csr<TS, CS>(tb.xp_ptr, tb.xp_col, tb.xp_val, v, vs, tmp, 1, tb.M, lane);
-    __syncwarp();
-    w_dz<TS, CS>(tmp, 1, csb, +1, tb, lane);
-    __syncwarp();
-    w_csr<TS, CS>(tb.xm_ptr, tb.xm_col, tb.xm_val, tmp, 1, v, vs, tb.M, lane);
-    __syncwarp();
-    w_dz<TS, CS>(v, vs, csa, +1, tb, lane);
-    __syncwarp();
 }
 
 template <typename X> __device__ __forceinline__ void stage(X* dst, const X* src, int n) {
@@ -140,80 +168,33 @@ template <typename X> __device__ __forceinline__ void stage(X* dst, const X* src
 }
 
 template <typename T, int N>
-__global__ void __launch_bounds__(kSolveWarpsMax * 32) zfft_solve(SolveArgs<T> a) {
+__global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1) zfft_solve(SolveArgs<T> a) {
     using C = typename cvec<T>::t;
     constexpr int NP = N + 1;
     const SolveTablesT<T>& g = a.tab;
     const int M = g.M, L = g.L;
-    const int nw = blockDim.x / 32, warp = threadIdx.x / 32, lane = threadIdx.x % 32;
     const int correct = a.correct;
-    const SolveSmem sm = solve_smem(N, M, L, nw, g.npairs, g.nnz, g.ndr, sizeof(T), correct);
+    const SolveSmem sm = solve_smem(N, M, L, g.ndr, sizeof(T), correct);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* col = reinterpret_cast<C*>(smem_raw + sm.col);
     C* tw = reinterpret_cast<C*>(smem_raw + sm.tw);
     T* csa = reinterpret_cast<T*>(smem_raw + sm.csa);
     float* csaf = reinterpret_cast<float*>(smem_raw + sm.csaf);
-    WTab<T> tb;
-    tb.L = L;
-    tb.M = M;
-    tb.npairs = g.npairs;
-    int16_t* s_pairs = reinterpret_cast<int16_t*>(smem_raw + sm.pairs);
-    int* s_xpp = reinterpret_cast<int*>(smem_raw + sm.xp_ptr);
-    int16_t* s_xpc = reinterpret_cast<int16_t*>(smem_raw + sm.xp_col);
-    T* s_xpv = reinterpret_cast<T*>(smem_raw + sm.xp_val);
-    int* s_xmp = reinterpret_cast<int*>(smem_raw + sm.xm_ptr);
-    int16_t* s_xmc = reinterpret_cast<int16_t*>(smem_raw + sm.xm_col);
-    T* s_xmv = reinterpret_cast<T*>(smem_raw + sm.xm_val);
     T* s_zoff = reinterpret_cast<T*>(smem_raw + sm.zoff);
-    stage(s_pairs, g.pairs, 3 * g.npairs);
-    stage(s_xpp, g.xp_ptr, M + 1);
-    stage(s_xpc, g.xp_col, g.nnz);
-    stage(s_xpv, g.xp_val, g.nnz);
-    stage(s_xmp, g.xm_ptr, M + 1);
-    stage(s_xmc, g.xm_col, g.nnz);
-    stage(s_xmv, g.xm_val, g.nnz);
+    float* s_zofff = reinterpret_cast<float*>(smem_raw + sm.zofff);
+    int* s_drp = reinterpret_cast<int*>(smem_raw + sm.dr_ptr);
+    int16_t* s_drc = reinterpret_cast<int16_t*>(smem_raw + sm.dr_col);
+    int8_t* s_dra = reinterpret_cast<int8_t*>(smem_raw + sm.dr_axis);
+    float* s_drv = reinterpret_cast<float*>(smem_raw + sm.dr_valf);
+    float2* corr = reinterpret_cast<float2*>(smem_raw + sm.corr);
     stage(s_zoff, g.zoff, M);
-    tb.pairs = s_pairs;
-    tb.xp_ptr = s_xpp;
-    tb.xp_col = s_xpc;
-    tb.xp_val = s_xpv;
-    tb.xm_ptr = s_xmp;
-    tb.xm_col = s_xmc;
-    tb.xm_val = s_xmv;
-    tb.zoff = s_zoff;
-    WTab<float> tf;
-    int* s_drp = nullptr;
-    int16_t* s_drc = nullptr;
-    int8_t* s_dra = nullptr;
-    float* s_drv = nullptr;
     if (correct) {
-        float* s_xpvf = reinterpret_cast<float*>(smem_raw + sm.xp_valf);
-        float* s_xmvf = reinterpret_cast<float*>(smem_raw + sm.xm_valf);
-        float* s_zofff = reinterpret_cast<float*>(smem_raw + sm.zofff);
-        s_drp = reinterpret_cast<int*>(smem_raw + sm.dr_ptr);
-        s_drc = reinterpret_cast<int16_t*>(smem_raw + sm.dr_col);
-        s_dra = reinterpret_cast<int8_t*>(smem_raw + sm.dr_axis);
-        s_drv = reinterpret_cast<float*>(smem_raw + sm.dr_valf);
-        stage(s_xpvf, g.xp_valf, g.nnz);
-        stage(s_xmvf, g.xm_valf, g.nnz);
         stage(s_zofff, g.zofff, M);
         stage(s_drp, g.dr_ptr, M + 1);
         stage(s_drc, g.dr_col, g.ndr);
         stage(s_dra, g.dr_axis, g.ndr);
         stage(s_drv, g.dr_valf, g.ndr);
-        tf.L = L;
-        tf.M = M;
-        tf.npairs = g.npairs;
-        tf.pairs = s_pairs;
-        tf.xp_ptr = s_xpp;
-        tf.xp_col = s_xpc;
-        tf.xp_val = s_xpvf;
-        tf.xm_ptr = s_xmp;
-        tf.xm_col = s_xmc;
-        tf.xm_val = s_xmvf;
-        tf.zoff = s_zofff;
     }
-
     const int colid = blockIdx.x;
     const int kyi = colid / a.nkx, kxi = colid % a.nkx;
     const int ix = fold_n(kxi, N), iy = fold_n(kyi, N);
@@ -228,10 +209,8 @@ __global__ void __launch_bounds__(kSolveWarpsMax * 32) zfft_solve(SolveArgs<T> a
         for (int m = 0; m <= L; ++m) {
             csa[2 * m] = (T)cm;
             csa[2 * m + 1] = (T)sm2;
-            if (correct) {
-                csaf[2 * m] = (float)cm;
-                csaf[2 * m + 1] = (float)sm2;
-            }
+            csaf[2 * m] = (float)cm;
+            csaf[2 * m + 1] = (float)sm2;
             const double cn = cm * ca - sm2 * sa, sn = sm2 * ca + cm * sa;
             cm = cn;
             sm2 = sn;
@@ -240,81 +219,86 @@ __global__ void __launch_bounds__(kSolveWarpsMax * 32) zfft_solve(SolveArgs<T> a
     __syncthreads();
     fft_nat2perm<N, -1>(col, M, 1, NP, tw);
 
-    C* wtmp = reinterpret_cast<C*>(smem_raw + sm.wtmp) + (size_t)warp * M;
-    float2* wrf = reinterpret_cast<float2*>(smem_raw + sm.wrf) + (size_t)warp * M;
-    float2* wtmf = reinterpret_cast<float2*>(smem_raw + sm.wtmf) + (size_t)warp * M;
-    // per-kz geometry of this column, computed once: cos/sin(m beta) for
-    // m = 0..L and t = sigma ds |k| (stride 2(L+1)+1), FP32 copies + kz
-    const int gs = 2 * (L + 1) + 1, gsf = 2 * (L + 1) + 2;
-    T* geo = reinterpret_cast<T*>(smem_raw + sm.wcsb);
-    float* geof = reinterpret_cast<float*>(smem_raw + sm.wcsbf);
-    for (int p = threadIdx.x; p < N; p += blockDim.x) {
-        const int iz = fold_n(perm_index<N>(p), N);
-        const double kz = iz * a.kf[2];
-        const double kn = sqrt(rho * rho + kz * kz);
-        const double cb = kn > 0 ? kz / kn : 1.0, sb = kn > 0 ? rho / kn : 0.0;
-        T* gp = geo + (size_t)p * gs;
-        float* gf = geof + (size_t)p * gsf;
-        double cm = 1.0, sm2 = 0.0;
-        for (int m = 0; m <= L; ++m) {
-            gp[2 * m] = (T)cm;
-            gp[2 * m + 1] = (T)sm2;
-            if (correct) {
-                gf[2 * m] = (float)cm;
-                gf[2 * m + 1] = (float)sm2;
-            }
-            const double cn = cm * cb - sm2 * sb, sn = sm2 * cb + cm * sb;
-            cm = cn;
-            sm2 = sn;
+    // Work split: thread t owns kz position p = t % N and part t / N of its
+    // solve (a greedy balance of the degree blocks and of the m systems
+    // over S = blockDim / N parts); the parts meet at CTA barriers.
+    const int S = max(1, (int)blockDim.x / N);
+    unsigned* masks = reinterpret_cast<unsigned*>(smem_raw + sm.masks);  // [2][S]: l blocks, m systems
+    if (threadIdx.x == 0) {
+        float load[32];
+        for (int q = 0; q < S; ++q) {
+            masks[q] = 0u;
+            masks[S + q] = 0u;
+            load[q] = 0.f;
         }
-        gp[2 * (L + 1)] = (T)(a.sigma * a.ds * kn);
-        if (correct) {
-            gf[2 * (L + 1)] = (float)(a.sigma * a.ds * kn);
-            gf[2 * (L + 1) + 1] = (float)kz;
+        for (int l = L; l >= 0; --l) {  // costliest first
+            int best = 0;
+            for (int q = 1; q < S; ++q)
+                if (load[q] < load[best]) best = q;
+            masks[best] |= 1u << l;
+            load[best] += (float)(l * l + 3 * l + 1);
+        }
+        for (int q = 0; q < S; ++q) load[q] = 0.f;
+        for (int m = 0; m <= L; ++m) {
+            int best = 0;
+            for (int q = 1; q < S; ++q)
+                if (load[q] < load[best]) best = q;
+            masks[S + best] |= 1u << m;
+            load[best] += (float)((L - m + 1) * (m > 0 ? 2 : 1));
         }
     }
     __syncthreads();
+    const int p = threadIdx.x % N, part = threadIdx.x / N;
+    const bool active = part < S && (int)threadIdx.x < N * S;
+    const unsigned lmask = active ? masks[part] : 0u, mmask = active ? masks[S + part] : 0u;
     const T c0 = (T)a.c0, dcoef = (T)a.dcoef;
-    const float kxf = (float)kx, kyf = (float)ky;
-    for (int p = warp; p < N; p += nw) {
-        const int iz = fold_n(perm_index<N>(p), N);
-        const T* wcsb = geo + (size_t)p * gs;
-        const T t = wcsb[2 * (L + 1)];
-        const T* pivrow = a.pivtab ? a.pivtab + (size_t)(ix * ix + iy * iy + iz * iz) * a.npiv : nullptr;
-        C* v = col + p;
-        w_cov_solve<T, C>(v, NP, wtmp, tb, csa, wcsb, t, c0, dcoef, pivrow, lane);
-        if (correct) {
-            // x -= G_cov^-1 (i sigma ds (k . dR) x), in FP32: the vector is
-            // rounded to FP32 once, the matvec and the solve run in FP32
-            const float* wcsbf = geof + (size_t)p * gsf;
-            const float sds = (float)(a.sigma * a.ds);
-            const float kk[3] = {kxf, kyf, wcsbf[2 * (L + 1) + 1]};
-            for (int i = lane; i < M; i += 32) {
-                const C x = v[i * NP];
-                wtmf[i] = make_float2((float)x.x, (float)x.y);
-            }
-            __syncwarp();
-            for (int i = lane; i < M; i += 32) {
+    const int iz = fold_n(perm_index<N>(p), N);
+    const double kz = iz * a.kf[2];
+    const double kn = sqrt(rho * rho + kz * kz);
+    const double cb = kn > 0 ? kz / kn : 1.0, sb = kn > 0 ? rho / kn : 0.0;
+    const T t = (T)(a.sigma * a.ds * kn);
+    const T* pivrow = a.pivtab ? a.pivtab + (size_t)(ix * ix + iy * iy + iz * iz) * a.npiv : nullptr;
+    C* v = col + p;
+    rot_all<T>(v, NP, L, csa, (T)cb, (T)sb, 1, lmask);
+    __syncthreads();
+    tridiag_all<T>(v, NP, L, t, c0, dcoef, s_zoff, pivrow, mmask);
+    __syncthreads();
+    rot_all<T>(v, NP, L, csa, (T)cb, (T)sb, 0, lmask);
+    __syncthreads();
+    if (correct) {
+        // x -= G_cov^-1 (i sigma ds (k . dR) x), in FP32
+        const float sds = (float)(a.sigma * a.ds);
+        const float kk[3] = {(float)kx, (float)ky, (float)kz};
+        float2* r = corr + p;
+        for (int l = 0; l <= L; ++l) {
+            if (!((lmask >> l) & 1u)) continue;
+            for (int i = l * l; i < (l + 1) * (l + 1); ++i) {
                 float ax = 0.f, ay = 0.f;
                 for (int e = s_drp[i]; e < s_drp[i + 1]; ++e) {
                     const float gv = kk[s_dra[e]] * s_drv[e];
-                    const float2 x = wtmf[s_drc[e]];
-                    ax = fmaf(gv, x.x, ax);
-                    ay = fmaf(gv, x.y, ay);
+                    const C x = v[s_drc[e] * NP];
+                    ax = fmaf(gv, (float)x.x, ax);
+                    ay = fmaf(gv, (float)x.y, ay);
                 }
-                wrf[i] = make_float2(-sds * ay, sds * ax);
+                r[i * N] = make_float2(-sds * ay, sds * ax);
             }
-            __syncwarp();
-            w_cov_solve<float, float2>(wrf, 1, wtmf, tf, csaf, wcsbf, wcsbf[2 * (L + 1)], (float)a.c0, (float)a.dcoef,
-                                       nullptr, lane);
-            for (int i = lane; i < M; i += 32) {
-                const float2 r = wrf[i];
+        }
+        __syncthreads();
+        rot_all<float>(r, N, L, csaf, (float)cb, (float)sb, 1, lmask);
+        __syncthreads();
+        tridiag_all<float>(r, N, L, (float)t, (float)a.c0, (float)a.dcoef, s_zofff, nullptr, mmask);
+        __syncthreads();
+        rot_all<float>(r, N, L, csaf, (float)cb, (float)sb, 0, lmask);
+        __syncthreads();
+        for (int l = 0; l <= L; ++l) {
+            if (!((lmask >> l) & 1u)) continue;
+            for (int i = l * l; i < (l + 1) * (l + 1); ++i) {
+                const float2 q = r[i * N];
                 C x = v[i * NP];
-                x.x -= (T)r.x;
-                x.y -= (T)r.y;
+                x.x -= (T)q.x;
+                x.y -= (T)q.y;
                 v[i * NP] = x;
             }
-            __syncwarp();
         }
     }
     __syncthreads();
@@ -347,21 +331,9 @@ __global__ void pivot_table(T* out, int nkeys, int L, double c0, double dcoef, d
     }
 }
 
-// warps per CTA: 16 when their per-warp buffers fit next to the column,
-// else 8
-template <typename T> int solve_warps(const SolveArgs<T>& a) {
-    const int N = 2 * (a.nkx - 1);
-    for (int nw = kSolveWarpsMax; nw >= 8; nw /= 2)
-        if (solve_smem(N, a.tab.M, a.tab.L, nw, a.tab.npairs, a.tab.nnz, a.tab.ndr, sizeof(T), a.correct).total <=
-            227 * 1024)
-            return nw;
-    return 8;
-}
-
 template <typename T> size_t solve_smem_bytes(const SolveArgs<T>& a) {
     const int N = 2 * (a.nkx - 1);
-    return solve_smem(N, a.tab.M, a.tab.L, solve_warps(a), a.tab.npairs, a.tab.nnz, a.tab.ndr, sizeof(T), a.correct)
-        .total;
+    return solve_smem(N, a.tab.M, a.tab.L, a.tab.ndr, sizeof(T), a.correct).total;
 }
 
 template <typename T, int N> static cudaError_t launch_solve_n(const SolveArgs<T>& a, cudaStream_t st) {
@@ -370,9 +342,7 @@ template <typename T, int N> static cudaError_t launch_solve_n(const SolveArgs<T
         cudaFuncSetAttribute(zfft_solve<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr_done = true;
     }
-    const int nw = solve_warps<T>(a);
-    const size_t bytes = solve_smem_bytes<T>(a);
-    zfft_solve<T, N><<<a.nkx * N, nw * 32, bytes, st>>>(a);
+    zfft_solve<T, N><<<a.nkx * N, kSolveThreads, solve_smem_bytes<T>(a), st>>>(a);
     return cudaGetLastError();
 }
 
