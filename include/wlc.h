@@ -55,7 +55,7 @@ enum { WLC_LIT_REAL4 = 0, WLC_LIT_REAL8 = 1 };
  * (global_parameters.f90:32,52-60), with one L for all blocks. */
 typedef struct wlc_params {
     int32_t n[3];       /* SIDEx, SIDEy, SIDEz (even)                              */
-    int32_t lmax;       /* L: harmonics l = 0..L, M = (L+1)^2 coefficients          */
+    int32_t lmax;       /* L <= 12: harmonics l = 0..L, M = (L+1)^2 coefficients    */
     int32_t nmax;       /* Nmax contour steps, ds = 1/Nmax                          */
     int32_t ns[3];      /* NA, NB, NC (even, NA+NB+NC = Nmax, initialize_mod.f90:190) */
     double dx[3];       /* grid spacing dx, dy, dz (box edge / SIDE)                */
@@ -109,6 +109,39 @@ int wlc_density(wlc_ctx* ctx, double* phi, double* junc, double* s_op, double* l
 /* free_energy() (SCFT_Density_FE.f90:273-342, three-block form): uses the
  * last wlc_density result and the current fields. */
 int wlc_free_energy(wlc_ctx* ctx, double* fe);
+
+/* Field-update parameters (the reference's iteration constants,
+ * global_parameters.f90:126-139, input.txt line 8, SCFT_main.f90:41). */
+typedef struct wlc_mix_params {
+    int32_t anderson_depth;   /* Anderson_nim_AB: history depth (1..10)                   */
+    int32_t num_simple;       /* Num_simple_mixing_AB = 20: simple-mixing iterations      */
+    double lambda_simple;     /* lanbtwA = lanbtwB = 0.1                                   */
+    double lambda_anderson;   /* lambda_WAB_anderson = 0.1                                 */
+    double tol;               /* CC = 1e-4: every block error below it means converged     */
+    int32_t min_iter;         /* 20: converged stays 0 while n_iter < min_iter             */
+    int32_t relax_iter;       /* 150: from this n_iter on (nmu == 0 only) ...              */
+    double relax_tol;         /* ... 5e-4 is enough; relax_iter <= 0 disables it           */
+    int32_t reserved[4];
+} wlc_mix_params;
+
+/* iterate(converge) (AB_iterate, SCFT_iterate.f90:27-334, three-block
+ * form): from the last wlc_density result, update the fields on the device
+ * by simple mixing (n_iter <= num_simple) or Anderson mixing (least squares
+ * in FP64 on the device).  With f_J = N_J/Nmax, the simple-mixing residual is
+ * dW_K = sum_J chi_KJ (phi_J - f_J) + (1/3) sum_J w_J - w_K and the Anderson
+ * output field w_K^out = sum_J chi_KJ phi_J + (1/3)(sum_J w_J - sum_KJ chi_KJ f_J)
+ * (both reduce to the reference's two-block formulas).
+ * err[0..2]: block errors (max |dW_K| while simple mixing,
+ * sqrt(<dW_K,dW_K>/<w_K^out,w_K^out>) with Anderson; global, not a mean of
+ * per-rank maxima); err[3]: incompressibility residual max |sum_K phi_K - 1|.
+ * n_iter counts the calls since creation, the last wlc_reset_mixing or a
+ * change of anderson_depth.  The fields of the next wlc_propagate are the
+ * updated ones; wlc_get_fields reads them. */
+int wlc_iterate(wlc_ctx* ctx, const wlc_mix_params* mp, double* err, int32_t* converged);
+int wlc_reset_mixing(wlc_ctx* ctx);
+
+/* Copy the current fields W_blk(0:LS,1:3) to the host (w[blk*nr + r]). */
+int wlc_get_fields(wlc_ctx* ctx, double* w);
 
 /* Copy one contour slice q_f(0:M-1,0:LS,s) (dir=+1) or q_star(...,s)
  * (dir=-1) to the host: out[r*M + i] (coefficient fastest, as the

@@ -188,7 +188,10 @@ class Oracle:
         return self.lib.orc_free_energy(self.h, float(lnq), _dp(phi))
 
     def simpson3(self, a):
-        a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.nr)
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if a.size != self.nr:  # several stacked fields: integrate their sum
+            a = a.reshape(-1, self.nr).sum(axis=0)
+        a = np.ascontiguousarray(a.reshape(self.nr))
         return self.lib.orc_simpson3(self.h, _dp(a))
 
     def bench_step(self, nk_sample):

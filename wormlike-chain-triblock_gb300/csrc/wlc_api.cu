@@ -2,6 +2,7 @@
 // owning its CUDA stream and device memory.  Sweep drivers follow
 // ABC_melt_driver (MDE_ABC.f90:8-88); density / free energy follow
 // SCFT_Density_FE_ABC.f90:3-271 and SCFT_Density_FE.f90:273-342.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -10,6 +11,8 @@
 
 #include "wlc.h"
 #include "wlc_internal.h"
+#include "wlc_mix.h"
+#include "wlc_rot_gen.cuh"
 #include "wlc_reduce.h"
 #include "wlc_step.h"
 
@@ -59,6 +62,11 @@ struct wlc_ctx {
     bool timing = false;
     std::vector<cudaEvent_t> ev;
     double tms[4] = {0, 0, 0, 0};
+    // field update (wlc_iterate)
+    int mix_iter = 0, mix_depth = -1;
+    double* wout_hist = nullptr;  // [depth+1][3][nr]
+    double* dw_hist = nullptr;    // [depth+1][3][nr]
+    double* mixbuf = nullptr;     // partials / results / coefficients
 };
 
 static int set_err(wlc_ctx* c, int code, const std::string& msg) {
@@ -204,8 +212,8 @@ static int validate(const wlc_params* p, std::string& why) {
         why = buf;
         return WLC_E_UNSUPPORTED;
     }
-    if (p->lmax < 0 || p->lmax > 15) {
-        why = "lmax must be in [0, 15]";
+    if (p->lmax < 0 || p->lmax > kRotLmax) {
+        why = "lmax must be in [0, 12] (the rotation codelets cover l <= 12)";
         return WLC_E_PARAM;
     }
     if (p->nmax < 3) {
@@ -803,4 +811,139 @@ extern "C" int wlc_mde_one_step(wlc_ctx* c, int32_t g_index, const double* pr, d
         for (auto& e : c->ev) CK(cudaEventCreate(&e));
     }
     return c->fp32 ? one_step_impl<float>(c, k, pr, q_out) : one_step_impl<double>(c, k, pr, q_out);
+}
+
+// ------------------------------------------------------------ field update
+static int anderson_index(int i, int nr) {  // Anderson_index, SCFT_iterate.f90:1-25
+    int a = i % (nr + 1);
+    if (i < 0) {
+        a = nr + 1 + a;
+        if (a == nr + 1) a = 0;
+    }
+    return a;
+}
+
+static void dfree(wlc_ctx* c, void* p) {
+    if (!p) return;
+    for (size_t i = 0; i < c->allocs.size(); ++i)
+        if (c->allocs[i] == p) {
+            c->allocs.erase(c->allocs.begin() + (long)i);
+            break;
+        }
+    cudaFree(p);
+}
+
+extern "C" int wlc_reset_mixing(wlc_ctx* c) {
+    if (!ready(c)) return WLC_E_STATE;
+    c->mix_iter = 0;
+    return WLC_OK;
+}
+
+extern "C" int wlc_get_fields(wlc_ctx* c, double* w) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!w) return set_err(c, WLC_E_PARAM, "w is null");
+    if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must come first");
+    CK(cudaMemcpyAsync(w, c->w, sizeof(double) * 3 * (size_t)c->nr, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return WLC_OK;
+}
+
+extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, int32_t* converged) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!mp || !err || !converged) return set_err(c, WLC_E_PARAM, "null argument");
+    if (!c->have_density) return set_err(c, WLC_E_STATE, "wlc_density must precede wlc_iterate");
+    const int depth = mp->anderson_depth;
+    if (depth < 1 || depth > kMaxAnderson) return set_err(c, WLC_E_PARAM, "anderson_depth must be in 1..10");
+    if (mp->num_simple < 1) return set_err(c, WLC_E_PARAM, "num_simple must be >= 1");
+    const int64_t nr = c->nr;
+    const size_t slot = 3 * (size_t)nr;
+    int rc;
+    if (c->mix_depth != depth) {  // (re)allocate the history; a depth change restarts the mixing
+        dfree(c, c->wout_hist);
+        dfree(c, c->dw_hist);
+        c->wout_hist = c->dw_hist = nullptr;
+        c->mix_depth = -1;
+        double* p;
+        if ((rc = dalloc(c, &p, sizeof(double) * slot * (depth + 1)))) return rc;
+        c->wout_hist = p;
+        if ((rc = dalloc(c, &p, sizeof(double) * slot * (depth + 1)))) return rc;
+        c->dw_hist = p;
+        if (!c->mixbuf) {
+            if ((rc = dalloc(c, &p, sizeof(double) * ((4 + kMaxMixAcc) * kMixBlocks + 256)))) return rc;
+            c->mixbuf = p;
+        }
+        c->mix_depth = depth;
+        c->mix_iter = 0;
+    }
+    double* maxpart = c->mixbuf;                    // [4][kMixBlocks]
+    double* dotpart = c->mixbuf + 4 * kMixBlocks;   // [kMaxMixAcc][kMixBlocks]
+    double* res = dotpart + kMaxMixAcc * kMixBlocks;  // 0..3 maxima, 8.. Anderson sums, 160.. coefficients
+    const int n = ++c->mix_iter;
+    const int ns = mp->num_simple;
+    const int k = n <= ns ? 0 : (n - ns) % (depth + 1);
+    double* wout = c->wout_hist + (size_t)k * slot;
+    double* dw = c->dw_hist + (size_t)k * slot;
+    MixChi chi;
+    chi.c[0][0] = chi.c[1][1] = chi.c[2][2] = 0.0;
+    chi.c[0][1] = chi.c[1][0] = c->p.chi[0];  // AB
+    chi.c[0][2] = chi.c[2][0] = c->p.chi[1];  // AC
+    chi.c[1][2] = chi.c[2][1] = c->p.chi[2];  // BC
+    for (int J = 0; J < 3; ++J) chi.f[J] = (double)c->p.ns[J] / (double)c->p.nmax;
+    chi.fsum = 0.0;
+    for (int K = 0; K < 3; ++K) {
+        chi.cf[K] = chi.c[K][0] * chi.f[0] + chi.c[K][1] * chi.f[1] + chi.c[K][2] * chi.f[2];
+        chi.fsum += chi.cf[K];
+    }
+    double h[96];
+    if (n <= ns) {  // simple mixing; the last one also fills history slot 0 (SCFT_iterate.f90:167-197)
+        launch_mix_out(c->phi, c->w, chi, nr, n == ns ? kMixSimpleStore : kMixSimple, mp->lambda_simple, wout, dw,
+                       maxpart, res, c->st);
+        c->launches += 2;
+        CK(cudaMemcpyAsync(h, res, sizeof(double) * 4, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        for (int q = 0; q < 4; ++q) err[q] = h[q];
+    } else {  // Anderson mixing (SCFT_iterate.f90:200-331)
+        launch_mix_out(c->phi, c->w, chi, nr, kMixStore, 0.0, wout, dw, maxpart, res, c->st);
+        const int nrt = std::min(n - ns, depth);
+        int km[kMaxAnderson];
+        AndersonSlots sl;
+        sl.dwk = dw;
+        sl.woutk = wout;
+        for (int m = 1; m <= nrt; ++m) {
+            km[m - 1] = anderson_index(k - m, depth);
+            sl.dwm[m - 1] = c->dw_hist + (size_t)km[m - 1] * slot;
+        }
+        for (int m = nrt; m < kMaxAnderson; ++m) sl.dwm[m] = dw;
+        MixGrid g;
+        for (int a = 0; a < 3; ++a) {
+            g.n[a] = c->N;
+            g.d[a] = c->p.dx[a];
+        }
+        const int nacc = anderson_acc_count(nrt);
+        launch_anderson_dots(sl, nrt, g, nr, c->vol, dotpart, res + 8, c->st);
+        launch_anderson(res + 8, nrt, res + 160, c->w, c->wout_hist, c->dw_hist, (int64_t)slot, k, km,
+                        mp->lambda_anderson, (int64_t)slot, c->st);
+        c->launches += 6;
+        CK(cudaMemcpyAsync(h, res, sizeof(double) * (8 + nacc), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        const double* nrm = h + 8 + (nacc - 6);
+        for (int K = 0; K < 3; ++K) err[K] = nrm[2 * K + 1] != 0.0 ? std::sqrt(std::fabs(nrm[2 * K] / nrm[2 * K + 1])) : 0.0;
+        err[3] = h[3];
+    }
+    // the fields changed: refresh the BDF3 coefficient planes
+    const double third = lit_third(c->real4);
+    if (c->fp32)
+        launch_make_cf<float>(c->w, (float*)c->cf, c->ds, third, c->nr, c->st);
+    else
+        launch_make_cf<double>(c->w, (double*)c->cf, c->ds, third, c->nr, c->st);
+    c->launches++;
+    CK(cudaGetLastError());
+    // convergence test (SCFT_iterate.f90:1124-1160) and the minimum iteration
+    // count of the driver loop (SCFT_control.f90:270-272)
+    const bool strict = err[0] < mp->tol && err[1] < mp->tol && err[2] < mp->tol;
+    const bool relaxed = c->p.nmu == 0.0 && mp->relax_iter > 0 && n >= mp->relax_iter && err[0] < mp->relax_tol &&
+                         err[1] < mp->relax_tol && err[2] < mp->relax_tol;
+    *converged = ((strict || relaxed) && n >= mp->min_iter) ? 1 : 0;
+    c->have_fwd = c->have_bwd = c->have_density = false;
+    return WLC_OK;
 }

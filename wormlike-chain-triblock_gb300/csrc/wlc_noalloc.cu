@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "wlc.h"
+#include "wlc_rot_gen.cuh"
 #include "wlc_internal.h"
 #include "wlc_step.h"
 
@@ -146,8 +147,8 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
     if (p->precision != WLC_FP64) return fail(errbuf, errlen, WLC_E_UNSUPPORTED, "only WLC_FP64 is built here");
     if (p->n[0] != p->n[1] || p->n[1] != p->n[2] || !supported_n(p->n[0]))
         return fail(errbuf, errlen, WLC_E_UNSUPPORTED, "grid must be cubic with a compiled edge length");
-    if (p->lmax < 0 || p->lmax > 15 || p->nmax < 1)
-        return fail(errbuf, errlen, WLC_E_PARAM, "lmax must be in [0, 15] and nmax >= 1");
+    if (p->lmax < 0 || p->lmax > kRotLmax || p->nmax < 1)
+        return fail(errbuf, errlen, WLC_E_PARAM, "lmax must be in [0, 12] and nmax >= 1");
     if (p->literals != WLC_LIT_REAL4 && p->literals != WLC_LIT_REAL8)
         return fail(errbuf, errlen, WLC_E_PARAM, "literals must be WLC_LIT_REAL4 or WLC_LIT_REAL8");
     for (int a = 0; a < 3; ++a)

@@ -34,7 +34,7 @@ ERRORS = {-1: "WLC_E_PARAM", -2: "WLC_E_ALLOC", -3: "WLC_E_CUDA", -4: "WLC_E_STA
 SYMBOLS = ["wlc_abi_version", "wlc_create", "wlc_destroy", "wlc_last_error", "wlc_set_box",
            "wlc_set_fields", "wlc_propagate", "wlc_density", "wlc_free_energy", "wlc_get_q",
            "wlc_set_q", "wlc_init_pr", "wlc_mde_one_step", "wlc_launch_count", "wlc_stream",
-           "wlc_enable_timing", "wlc_last_timing"]
+           "wlc_enable_timing", "wlc_last_timing", "wlc_iterate", "wlc_reset_mixing", "wlc_get_fields"]
 
 
 class WlcError(RuntimeError):
@@ -49,6 +49,24 @@ class Params(ctypes.Structure):
                 ("kappa", ctypes.c_double * 3), ("chi", ctypes.c_double * 3), ("nmu", ctypes.c_double),
                 ("precision", ctypes.c_int32), ("literals", ctypes.c_int32),
                 ("store_qstar", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+
+
+class MixParams(ctypes.Structure):
+    """wlc_mix_params: the reference's iteration constants
+    (global_parameters.f90:69,126-139, SCFT_main.f90:41)."""
+    _fields_ = [("anderson_depth", ctypes.c_int32), ("num_simple", ctypes.c_int32),
+                ("lambda_simple", ctypes.c_double), ("lambda_anderson", ctypes.c_double),
+                ("tol", ctypes.c_double), ("min_iter", ctypes.c_int32), ("relax_iter", ctypes.c_int32),
+                ("relax_tol", ctypes.c_double), ("reserved", ctypes.c_int32 * 4)]
+
+
+def mix_params(anderson_depth=5, num_simple=20, lambda_simple=0.1, lambda_anderson=0.1, tol=1e-4,
+               min_iter=20, relax_iter=150, relax_tol=5e-4):
+    m = MixParams()
+    m.anderson_depth, m.num_simple = int(anderson_depth), int(num_simple)
+    m.lambda_simple, m.lambda_anderson, m.tol = float(lambda_simple), float(lambda_anderson), float(tol)
+    m.min_iter, m.relax_iter, m.relax_tol = int(min_iter), int(relax_iter), float(relax_tol)
+    return m
 
 
 def lib_path():
@@ -90,6 +108,9 @@ def load(build_if_missing=True):
     lib.wlc_stream.restype = P
     lib.wlc_enable_timing.argtypes = [P, I]
     lib.wlc_last_timing.argtypes = [P, Dp]
+    lib.wlc_iterate.argtypes = [P, ctypes.POINTER(MixParams), Dp, ctypes.POINTER(ctypes.c_int32)]
+    lib.wlc_reset_mixing.argtypes = [P]
+    lib.wlc_get_fields.argtypes = [P, Dp]
     _LIB = lib
     return lib
 
@@ -262,3 +283,42 @@ class Instance:
         t = np.zeros(4)
         self._check(self.lib.wlc_last_timing(self.h, _dp(t)))
         return t
+
+    # ---------------------------------------------------------- SCFT loop
+    def iterate(self, mix=None, **kw):
+        """iterate(converge) (SCFT_iterate.f90:27-334, three-block form) on the
+        device; returns (err[4], converged).  err[0..2] block errors, err[3]
+        max |sum_K phi_K - 1|."""
+        mp = mix if mix is not None else mix_params(**kw)
+        err = np.zeros(4)
+        conv = ctypes.c_int32(0)
+        self._check(self.lib.wlc_iterate(self.h, ctypes.byref(mp), _dp(err), ctypes.byref(conv)))
+        return err, bool(conv.value)
+
+    def reset_mixing(self):
+        self._check(self.lib.wlc_reset_mixing(self.h))
+
+    def get_fields(self):
+        w = np.empty((3, self.nr))
+        self._check(self.lib.wlc_get_fields(self.h, _dp(w)))
+        return w
+
+    def cal_scft(self, max_iter=5000, mix=None, callback=None, **kw):
+        """The SCFT loop of cal_scft (SCFT_control.f90:237-273): propagators,
+        density, free energy and field update until converged or max_iter
+        (MAXITS = 5000, global_parameters.f90:69) iterations.  Returns
+        dict(F, lnQ, n_iter, converged, history=[(F, err)])."""
+        mp = mix if mix is not None else mix_params(**kw)
+        hist = []
+        conv, n, d, fe = False, 0, None, float("nan")
+        while not conv and n < max_iter:
+            n += 1
+            self.MDE_q()
+            self.MDE_qstar()
+            d = self.density(want_junction=False)
+            fe = self.free_energy()
+            err, conv = self.iterate(mp)
+            hist.append((fe, err.copy()))
+            if callback is not None:
+                callback(n, fe, err)
+        return dict(F=fe, lnQ=d["lnQ"] if d else float("nan"), n_iter=n, converged=conv, history=hist)
