@@ -363,6 +363,72 @@ def run_profile_case(args):
     inst.close()
 
 
+def run_converge(args):
+    """Time-to-converged F at the bench workload: the SCFT loop (propagators,
+    densities, free energy, field update on the device) from the same seeded
+    cold start until every block residual is <= tol, for each form:
+      fp64       plain FP64 propagators throughout (the drop-in);
+      fp32sched  FP32 propagators until the residual falls below
+                 --switch-tol, then FP64 to the end (same fields and
+                 mixing history);
+      fp32       FP32 propagators throughout (reports where FP32 stalls).
+    FP64 Q, F, residuals and the Anderson least squares in every form.
+    Wall time includes everything; capped by --budget seconds per form."""
+    import torch
+    import wlc
+    wl = workload("fp64")
+    nr = wl["n"] ** 3
+    rng = np.random.default_rng(2024)
+    w0 = rng.normal(0.0, wl["w_sigma"], size=(3, nr))
+    mp = wlc.mix_params(anderson_depth=args.depth, num_simple=20, lambda_anderson=args.lambda_a, tol=args.tol,
+                        min_iter=20, relax_iter=0)
+    out = {"metric": "time-to-converged F (64^3, L=10, Ns=200, ABC; residual <= %g)" % args.tol,
+           "mixing": {"anderson_depth": args.depth, "num_simple": 20, "lambda_simple": 0.1,
+                      "lambda_anderson": args.lambda_a, "ramp": args.ramp}, "forms": {}}
+    for form in args.forms.split(","):
+        prec = wlc.WLC_FP64 if form == "fp64" else wlc.WLC_FP32
+        inst = wlc.Instance(wl["n"], wl["L"], wl["nmax"], wl["ns"], wl["dx"], wl["loa"], wl["kappa"], wl["chi"],
+                            precision=prec)
+        inst.set_fields(w0)
+        mp.lambda_anderson = args.lambda_a
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hist, switched, n, conv = [], None, 0, False
+        t_switch = None
+        while not conv and n < args.max_iter and time.perf_counter() - t0 < args.budget:
+            n += 1
+            if args.ramp and n > 20:  # lambda_A = max(lambda_a, 1 - 0.9^(n - 20))
+                mp.lambda_anderson = max(args.lambda_a, 1.0 - 0.9 ** (n - 20))
+            inst.MDE_q()
+            inst.MDE_qstar()
+            d = inst.density(want_junction=False)
+            fe = inst.free_energy()
+            err, conv = inst.iterate(mp)
+            hist.append([n, fe, d["lnQ"]] + [float(e) for e in err])
+            if form == "fp32sched" and switched is None and max(err[:3]) < args.switch_tol and n > 20:
+                inst.set_precision(wlc.WLC_FP64)
+                switched = n
+                t_switch = time.perf_counter() - t0
+        torch.cuda.synchronize()
+        secs = time.perf_counter() - t0
+        out["forms"][form] = {"converged": bool(conv), "iterations": n, "seconds": secs, "F": hist[-1][1],
+                              "lnQ": hist[-1][2], "residual": max(hist[-1][3:6]), "incompressibility": hist[-1][6],
+                              "switched_at": switched, "switch_seconds": t_switch,
+                              "s_per_iteration": secs / max(1, n)}
+        if args.history:
+            out["forms"][form]["history"] = hist
+        inst.close()
+        print(json.dumps({"form": form, **{k: v for k, v in out["forms"][form].items() if k != "history"}}),
+              flush=True)
+    f = out["forms"]
+    if "fp64" in f:
+        for k, v in f.items():
+            if k != "fp64":
+                v["F_rel_err_vs_fp64"] = abs(v["F"] - f["fp64"]["F"]) / abs(f["fp64"]["F"])
+                v["speedup_vs_fp64"] = f["fp64"]["seconds"] / v["seconds"]
+    print(json.dumps(out))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -372,9 +438,22 @@ def main():
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"])
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="small-footprint case for ncu captures")
+    ap.add_argument("--converge", action="store_true", help="time-to-converged F instead of steps/s")
+    ap.add_argument("--forms", default="fp32sched,fp64")
+    ap.add_argument("--tol", type=float, default=1e-6)
+    ap.add_argument("--switch-tol", type=float, default=1e-4)
+    ap.add_argument("--depth", type=int, default=5)
+    ap.add_argument("--max-iter", type=int, default=2000)
+    ap.add_argument("--budget", type=float, default=900.0, help="wall-time cap per form, seconds")
+    ap.add_argument("--history", action="store_true")
+    ap.add_argument("--lambda-a", type=float, default=0.1, help="Anderson mixing parameter")
+    ap.add_argument("--ramp", action="store_true", help="ramp lambda_A towards 1 after the simple phase")
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args)
+        return
+    if args.converge:
+        run_converge(args)
         return
     wl = workload(args.precision)
     if args.impl == "reference":

@@ -65,8 +65,15 @@ typedef struct wlc_params {
     double nmu;         /* Maier-Saupe NMu (0 disables the Theta term)              */
     int32_t precision;  /* WLC_FP64 (drop-in) or WLC_FP32 propagators               */
     int32_t literals;   /* WLC_LIT_REAL4 or WLC_LIT_REAL8                            */
-    int32_t store_qstar;/* 1: keep every q* slice (wlc_get_q on dir -1 works)       */
-    int32_t reserved[5];
+    int32_t store_qstar;/* 1: keep every q* slice (wlc_get_q / wlc_init_pr on dir -1);
+                           0: keep a 4-slice ring of q* and accumulate the densities
+                              during the backward sweep (half the memory);
+                           2: as 0, also accumulating the orientation tensor      */
+    int32_t q_checkpoint;/* 0: keep every q slice; K >= 3: keep the BDF3 history at
+                           every K-th slice and recompute each segment of q during
+                           the backward sweep (needs store_qstar 0 or 2; K ~ sqrt(3 Nmax)
+                           minimises memory, at one extra forward sweep)           */
+    int32_t reserved[4];
 } wlc_params;
 
 typedef struct wlc_ctx wlc_ctx;
@@ -142,6 +149,15 @@ int wlc_reset_mixing(wlc_ctx* ctx);
 
 /* Copy the current fields W_blk(0:LS,1:3) to the host (w[blk*nr + r]). */
 int wlc_get_fields(wlc_ctx* ctx, double* w);
+
+/* No counterpart in the reference (which is FP64 only).  Switch the
+ * propagator precision of an existing context between WLC_FP64 and WLC_FP32
+ * (precision schedules: FP32 sweeps far from convergence, FP64 to finish).
+ * Fields, mixing history and box are kept; propagator slices and the last
+ * density are invalidated.  The first switch to a precision builds its
+ * operator tables; switching FP32 -> FP64 in a context created FP32
+ * reallocates the propagator storage at twice the size. */
+int wlc_set_precision(wlc_ctx* ctx, int32_t precision);
 
 /* Copy one contour slice q_f(0:M-1,0:LS,s) (dir=+1) or q_star(...,s)
  * (dir=-1) to the host: out[r*M + i] (coefficient fastest, as the

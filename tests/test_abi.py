@@ -32,9 +32,17 @@ def test_abi_version():
 
 def test_params_struct_layout():
     # int32 n[3], lmax, nmax, ns[3]; double dx[3], loa, kappa[3], chi[3], nmu;
-    # int32 precision, literals, store_qstar, reserved[5]
+    # int32 precision, literals, store_qstar, q_checkpoint, reserved[4]
     assert ctypes.sizeof(wlc.Params) == 152
     assert wlc.Params.dx.offset == 32 and wlc.Params.precision.offset == 120
+    assert wlc.Params.q_checkpoint.offset == 132
+
+
+def test_mix_params_struct_layout():
+    # int32 anderson_depth, num_simple; double lambda_simple, lambda_anderson, tol;
+    # int32 min_iter, relax_iter; double relax_tol; int32 reserved[4]
+    assert ctypes.sizeof(wlc.MixParams) == 64
+    assert wlc.MixParams.tol.offset == 24 and wlc.MixParams.relax_tol.offset == 40
 
 
 def _create(**kw):
@@ -50,6 +58,8 @@ def _create(**kw):
     p.chi[:] = [15.0, 15.0, 15.0]
     p.precision = kw.get("precision", 0)
     p.literals = 0
+    p.store_qstar = kw.get("store_qstar", 1)
+    p.q_checkpoint = kw.get("q_checkpoint", 0)
     h = ctypes.c_void_p()
     rc = lib.wlc_create(ctypes.byref(p), ctypes.byref(h))
     msg = lib.wlc_last_error(h).decode() if h else ""
@@ -64,6 +74,11 @@ def _create(**kw):
     (dict(n=[10, 10, 10]), -6, "compiled"),
     (dict(lmax=20), -1, "lmax"),
     (dict(precision=7), -1, "precision"),
+    (dict(lmax=13), -1, "lmax"),                  # rotation codelets cover l <= 12
+    (dict(store_qstar=3), -1, "store_qstar"),
+    (dict(q_checkpoint=4), -1, "q_checkpoint"),   # checkpointing needs streamed densities
+    (dict(q_checkpoint=2, store_qstar=0), -1, "q_checkpoint"),
+    (dict(q_checkpoint=7, store_qstar=0), -1, "q_checkpoint"),  # > nmax
 ])
 def test_invalid_parameters_are_rejected_before_any_device_work(kw, code, text):
     rc, msg = _create(**kw)

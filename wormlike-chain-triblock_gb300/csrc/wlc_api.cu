@@ -38,8 +38,25 @@ struct wlc_ctx {
     ThetaLists thl{};
     JLists jl{};
     void* twg = nullptr;
+    // per-precision operator data ([0] FP64, [1] FP32); twg / pivtab /
+    // have_piv above alias the active one
+    struct PrecState {
+        bool built = false;
+        void* twg = nullptr;
+        void* pivtab = nullptr;
+        bool have_piv = false;
+        int piv_gen = -1;
+    } prec[2];
+    int box_gen = 0;   // incremented by every wlc_set_box
+    size_t elem = 0;   // bytes per real of the propagator buffers as allocated
+    // propagator storage: qf holds all Nmax+1 slices of q, or (q_checkpoint K
+    // > 0) a 4-slice ring, the BDF3 history triple at every K-th slice and a
+    // (K+2)-slice segment buffer; qb holds all slices of q* or (streamed
+    // densities) a 4-slice ring
     void* qf = nullptr;
     void* qb = nullptr;
+    int K = 0, nck = 0;
+    bool stream = false;
     void* phat = nullptr;
     void* cf = nullptr;
     void* work = nullptr;    // [M][nr] compute type: RHS / one-step scratch
@@ -47,12 +64,14 @@ struct wlc_ctx {
     double* w = nullptr;
     double* mop = nullptr;
     double* raw = nullptr;   // [3][nr]
-    double* junc = nullptr;  // [3][nr]
+    double* junc = nullptr;  // [3][nr] (unscaled)
+    double* juncs = nullptr; // [3][nr] scaled copy
     double* qend = nullptr;  // [nr]
     double* phi = nullptr;   // [3][nr]
     double* part = nullptr;  // [kS3Blocks]
     double* scal = nullptr;  // [8]
-    double* sraw = nullptr;  // [3][5][nr]
+    double* sraw = nullptr;  // [3][5][nr] (unscaled)
+    double* srs = nullptr;   // [3][5][nr] scaled copy
     double* ar = nullptr;    // [nr]
     double* stage = nullptr; // [M*nr] double, host transfer staging
     int* flag = nullptr;
@@ -250,6 +269,14 @@ static int validate(const wlc_params* p, std::string& why) {
         why = "literals must be WLC_LIT_REAL4 or WLC_LIT_REAL8";
         return WLC_E_PARAM;
     }
+    if (p->store_qstar < 0 || p->store_qstar > 2) {
+        why = "store_qstar must be 0, 1 or 2";
+        return WLC_E_PARAM;
+    }
+    if (p->q_checkpoint != 0 && (p->q_checkpoint < 3 || p->q_checkpoint > p->nmax || p->store_qstar == 1)) {
+        why = "q_checkpoint must be 0 or in [3, nmax], and needs store_qstar 0 or 2";
+        return WLC_E_PARAM;
+    }
     return WLC_OK;
 }
 
@@ -284,9 +311,11 @@ template <typename T> static int alloc_fields(wlc_ctx* c) {
     int rc;
     T* pt;
     C* pc;
-    if ((rc = dalloc(c, &pt, sizeof(T) * sl * (c->p.nmax + 1)))) return rc;
+    const size_t nqf = c->K > 0 ? (size_t)(4 + 3 * c->nck + c->K + 2) : (size_t)(c->p.nmax + 1);
+    const size_t nqb = c->stream ? 4 : (size_t)(c->p.nmax + 1);
+    if ((rc = dalloc(c, &pt, sizeof(T) * sl * nqf))) return rc;
     c->qf = pt;
-    if ((rc = dalloc(c, &pt, sizeof(T) * sl * (c->p.nmax + 1)))) return rc;
+    if ((rc = dalloc(c, &pt, sizeof(T) * sl * nqb))) return rc;
     c->qb = pt;
     if ((rc = dalloc(c, &pc, sizeof(C) * (size_t)c->nk * c->M))) return rc;
     c->phat = pc;
@@ -298,7 +327,76 @@ template <typename T> static int alloc_fields(wlc_ctx* c) {
         if ((rc = dalloc(c, &pt, sizeof(T) * sl))) return rc;
         c->msterm = pt;
     }
-    return build_twiddles<T>(c);
+    c->elem = sizeof(T);
+    return WLC_OK;
+}
+
+static int check_smem(wlc_ctx* c, bool fp32) {
+    const size_t sxy = fp32 ? smem_xy<float>(c->N) : smem_xy<double>(c->N);
+    int ndr = 0;
+    for (int a = 0; a < 3; ++a) ndr += (int)c->tab.dR[a].size();
+    const bool corr = !fp32 && ndr > 0;
+    const size_t ssv = solve_smem(c->N, c->M, c->L, ndr, fp32 ? 4 : 8, corr ? 1 : 0).total;
+    if (ssv > 227 * 1024 || sxy > 227 * 1024)
+        return set_err(c, WLC_E_UNSUPPORTED, "one coefficient column (M x N) does not fit in shared memory for "
+                                             "this (N, L, precision)");
+    return WLC_OK;
+}
+
+// Make precision T the active one: operator tables, twiddles and pivots of
+// T (built once, pivots rebuilt after a box change), propagator buffers wide
+// enough for T, coefficient planes refreshed from the fields.
+template <typename T> static int use_precision(wlc_ctx* c) {
+    constexpr int idx = sizeof(T) == 4 ? 1 : 0;
+    int rc;
+    if ((rc = check_smem(c, idx == 1))) return rc;
+    auto& ps = c->prec[idx];
+    if (!ps.built) {
+        if constexpr (idx == 1) {
+            if ((rc = build_solve_tables<float>(c, c->sf))) return rc;
+        } else {
+            if ((rc = build_solve_tables<double>(c, c->sd))) return rc;
+        }
+        if ((rc = build_twiddles<T>(c))) return rc;
+        ps.twg = c->twg;
+        void* pv = nullptr;
+        if ((rc = dalloc(c, (unsigned char**)&pv, (size_t)9 * c->nkeys * c->npiv * sizeof(T)))) return rc;
+        ps.pivtab = pv;
+        ps.built = true;
+        ps.piv_gen = -1;
+    }
+    c->fp32 = idx == 1;
+    c->p.precision = idx == 1 ? WLC_FP32 : WLC_FP64;
+    c->twg = ps.twg;
+    c->pivtab = ps.pivtab;
+    if (ps.piv_gen != c->box_gen) {
+        if ((rc = build_pivots<T>(c))) return rc;
+        ps.have_piv = c->have_piv;
+        ps.piv_gen = c->box_gen;
+    } else {
+        c->have_piv = ps.have_piv;
+    }
+    if (c->elem < sizeof(T)) {  // widen the propagator buffers
+        for (void** b : {&c->qf, &c->qb, &c->phat, &c->cf, &c->work, &c->msterm}) {
+            if (*b) {
+                for (size_t i = 0; i < c->allocs.size(); ++i)
+                    if (c->allocs[i] == *b) {
+                        c->allocs.erase(c->allocs.begin() + (long)i);
+                        break;
+                    }
+                cudaFree(*b);
+                *b = nullptr;
+            }
+        }
+        if ((rc = alloc_fields<T>(c))) return rc;
+    }
+    if (c->have_fields) {
+        launch_make_cf<T>(c->w, (T*)c->cf, c->ds, lit_third(c->real4), c->nr, c->st);
+        c->launches++;
+        CK(cudaGetLastError());
+    }
+    c->have_fwd = c->have_bwd = c->have_density = false;
+    return WLC_OK;
 }
 
 extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
@@ -327,22 +425,14 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
     c->nstart[0] = 0;
     c->nstart[1] = p->ns[0];
     c->nstart[2] = p->ns[0] + p->ns[1];
+    c->stream = p->store_qstar != 1;
+    c->K = p->q_checkpoint;
+    c->nck = c->K > 0 ? p->nmax / c->K : 0;
     *out = c;
     if (!build_basis_tables(c->L, c->real4, c->tab, why)) return set_err(c, WLC_E_SELFTEST, why);
-    const size_t sxy = c->fp32 ? smem_xy<float>(c->N) : smem_xy<double>(c->N);
-    {
-        int npairs = c->L * (c->L + 1) / 2, ndr = 0;
-        for (int a = 0; a < 3; ++a) ndr += (int)c->tab.dR[a].size();
-        const bool corr = !c->fp32 && ndr > 0;
-        (void)npairs;
-        const size_t ssv = solve_smem(c->N, c->M, c->L, ndr, c->fp32 ? 4 : 8, corr ? 1 : 0).total;
-        if (ssv > 227 * 1024 || sxy > 227 * 1024)
-            return set_err(c, WLC_E_UNSUPPORTED, "one coefficient column (M x N) does not fit in shared memory for "
-                                                 "this (N, L, precision)");
-    }
+    if ((rc = check_smem(c, c->fp32))) return rc;
     CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
     apply_box(c);
-    if ((rc = c->fp32 ? build_solve_tables<float>(c, c->sf) : build_solve_tables<double>(c, c->sd))) return rc;
     // Theta and J lists
     {
         std::vector<int16_t> tr, tcol;
@@ -387,15 +477,10 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
         if ((rc = upload(c, &pd, jv))) return rc;
         c->jl.val = pd;
     }
-    if ((rc = c->fp32 ? alloc_fields<float>(c) : alloc_fields<double>(c))) return rc;
     c->nkeys = 3 * (c->N / 2) * (c->N / 2) + 1;
     c->npiv = (c->L + 1) * (c->L + 2) / 2;
-    {
-        void* pv = nullptr;
-        if ((rc = dalloc(c, (unsigned char**)&pv, (size_t)9 * c->nkeys * c->npiv * (c->fp32 ? 4 : 8)))) return rc;
-        c->pivtab = pv;
-    }
-    if ((rc = c->fp32 ? build_pivots<float>(c) : build_pivots<double>(c))) return rc;
+    if ((rc = c->fp32 ? alloc_fields<float>(c) : alloc_fields<double>(c))) return rc;
+    if ((rc = c->fp32 ? use_precision<float>(c) : use_precision<double>(c))) return rc;
     const size_t nr = (size_t)c->nr;
     if ((rc = dalloc(c, &c->w, sizeof(double) * 3 * nr))) return rc;
     if ((rc = dalloc(c, &c->mop, sizeof(double) * 9 * nr))) return rc;
@@ -406,6 +491,8 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
     if ((rc = dalloc(c, &c->part, sizeof(double) * kS3Blocks))) return rc;
     if ((rc = dalloc(c, &c->scal, sizeof(double) * 8))) return rc;
     if ((rc = dalloc(c, &c->sraw, sizeof(double) * 15 * nr))) return rc;
+    if ((rc = dalloc(c, &c->srs, sizeof(double) * 15 * nr))) return rc;
+    if ((rc = dalloc(c, &c->juncs, sizeof(double) * 3 * nr))) return rc;
     if ((rc = dalloc(c, &c->ar, sizeof(double) * nr))) return rc;
     if ((rc = dalloc(c, &c->stage, sizeof(double) * (size_t)c->M * nr))) return rc;
     if ((rc = dalloc(c, &c->flag, sizeof(int)))) return rc;
@@ -434,10 +521,22 @@ extern "C" int wlc_set_box(wlc_ctx* c, double dx, double dy, double dz) {
     c->p.dx[1] = dy;
     c->p.dx[2] = dz;
     apply_box(c);
+    c->box_gen++;
     int rc = c->fp32 ? build_pivots<float>(c) : build_pivots<double>(c);
     if (rc) return rc;
+    auto& ps = c->prec[c->fp32 ? 1 : 0];
+    ps.have_piv = c->have_piv;
+    ps.piv_gen = c->box_gen;
     c->have_fwd = c->have_bwd = c->have_density = false;
     return WLC_OK;
+}
+
+extern "C" int wlc_set_precision(wlc_ctx* c, int32_t precision) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (precision != WLC_FP64 && precision != WLC_FP32)
+        return set_err(c, WLC_E_PARAM, "precision must be WLC_FP64 or WLC_FP32");
+    if ((precision == WLC_FP32) == c->fp32) return WLC_OK;
+    return precision == WLC_FP32 ? use_precision<float>(c) : use_precision<double>(c);
 }
 
 extern "C" int wlc_set_fields(wlc_ctx* c, const double* w, const double* m_op) {
@@ -527,42 +626,136 @@ static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h
 
 template <typename T> static int run_step(wlc_ctx* c, StepLaunch<T>& L, double c0, int slot) {
     L.solve.c0 = c0;
-    if (c->timing) L.events = &c->ev[4 * (size_t)slot];
+    L.events = (c->timing && slot >= 0) ? &c->ev[4 * (size_t)slot] : nullptr;
     cudaError_t e = launch_step<T>(c->N, L, c->st);
     c->launches += 3;
     if (e != cudaSuccess) return set_err(c, WLC_E_CUDA, std::string("step launch: ") + cudaGetErrorString(e));
     return WLC_OK;
 }
 
+// one contour step of either sweep: out = G^-1 . RHS(h1, h2, h3)
+template <typename T>
+static int contour_step(wlc_ctx* c, StepKind k, const T* h1, const T* h2, const T* h3, T* out, int slot) {
+    StepLaunch<T> L = make_launch<T>(c, k, h1, h2, h3, out);
+    if (std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop) {
+        launch_ms_term<T>(h1, h2, h3, k.order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M, c->nr,
+                          (T*)c->msterm, c->st);
+        c->launches++;
+        L.step.msterm = (const T*)c->msterm;
+    }
+    return run_step<T>(c, L, lit_c0(k.order, c->real4), slot);
+}
+
+// slice addressing of the storage modes
+template <typename T> static T* qf_ring(wlc_ctx* c, int s) {
+    return (T*)c->qf + (size_t)(s & 3) * (size_t)c->M * c->nr;
+}
+template <typename T> static T* qf_ckpt(wlc_ctx* c, int m, int j) {  // q(mK - 2 + j), m >= 1
+    return (T*)c->qf + (size_t)(4 + 3 * (m - 1) + j) * (size_t)c->M * c->nr;
+}
+template <typename T> static T* qf_seg(wlc_ctx* c, int idx) {  // segment slot idx = s - mK + 2
+    return (T*)c->qf + (size_t)(4 + 3 * c->nck + idx) * (size_t)c->M * c->nr;
+}
+// q(s) as the backward sweep sees it
+template <typename T> static T* qf_at(wlc_ctx* c, int s) {
+    if (c->K == 0) return (T*)c->qf + (size_t)s * (size_t)c->M * c->nr;
+    return qf_seg<T>(c, s - (s / c->K) * c->K + 2);
+}
+template <typename T> static T* qb_at(wlc_ctx* c, int s) {
+    return (T*)c->qb + (size_t)(c->stream ? (s & 3) : s) * (size_t)c->M * c->nr;
+}
+
+// recompute q over segment m (slices mK+1 .. min(mK+K-1, Nmax)) into the
+// segment buffer from the stored BDF3 history at mK (bit-identical to the
+// forward sweep: same kernels, same inputs)
+template <typename T> static int recompute_segment(wlc_ctx* c, int m) {
+    const size_t sl = (size_t)c->M * c->nr;
+    const int base = m * c->K, top = std::min(base + c->K - 1, c->p.nmax);
+    if (m == 0) {
+        launch_set_delta<T>(qf_seg<T>(c, 2), c->M, c->nr, c->st);
+        c->launches++;
+    } else {
+        CK(cudaMemcpyAsync(qf_seg<T>(c, 0), qf_ckpt<T>(c, m, 0), sizeof(T) * sl * 3, cudaMemcpyDeviceToDevice,
+                           c->st));
+    }
+    for (int s = base + 1; s <= top; ++s) {
+        const int order = s < 3 ? s : 3;
+        const int i = s - base + 2;
+        int rc = contour_step<T>(c, StepKind{order, 1, blk_fwd(c, s)}, qf_seg<T>(c, i - 1),
+                                 order >= 2 ? qf_seg<T>(c, i - 2) : nullptr, order >= 3 ? qf_seg<T>(c, i - 3) : nullptr,
+                                 qf_seg<T>(c, i), -1);
+        if (rc) return rc;
+    }
+    return WLC_OK;
+}
+
+static DensityArgs density_args(const wlc_ctx* c) {
+    DensityArgs d;
+    d.nr = c->nr;
+    d.M = c->M;
+    d.nmax = c->p.nmax;
+    for (int b = 0; b < 3; ++b) {
+        d.nstart[b] = c->nstart[b];
+        d.ns[b] = c->p.ns[b];
+    }
+    d.ds = c->ds;
+    return d;
+}
+
 template <typename T> static int sweep(wlc_ctx* c, int dir) {
     const size_t sl = (size_t)c->M * c->nr;
-    T* q = (T*)(dir > 0 ? c->qf : c->qb);
     const int nmax = c->p.nmax;
-    const bool ms = std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop;
     if (c->timing && c->ev.size() < 4 * (size_t)(nmax + 1)) {
         for (auto e : c->ev) cudaEventDestroy(e);
         c->ev.assign(4 * (size_t)(nmax + 1), nullptr);
         for (auto& e : c->ev) CK(cudaEventCreate(&e));
     }
-    const int s_init = dir > 0 ? 0 : nmax;
-    launch_set_delta<T>(q + (size_t)s_init * sl, c->M, c->nr, c->st);  // q(0)=delta / q*(Nmax)=delta
-    c->launches++;
-    for (int n = 1; n <= nmax; ++n) {
-        const int s = dir > 0 ? n : nmax - n;
-        const int order = n < 3 ? n : 3;
-        StepKind k{order, dir, dir > 0 ? blk_fwd(c, s) : blk_bwd(c, s)};
-        const T* h1 = q + (size_t)(s - dir) * sl;
-        const T* h2 = order >= 2 ? q + (size_t)(s - 2 * dir) * sl : nullptr;
-        const T* h3 = order >= 3 ? q + (size_t)(s - 3 * dir) * sl : nullptr;
-        StepLaunch<T> L = make_launch<T>(c, k, h1, h2, h3, q + (size_t)s * sl);
-        if (ms) {
-            launch_ms_term<T>(h1, h2, h3, order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M, c->nr,
-                              (T*)c->msterm, c->st);
-            c->launches++;
-            L.step.msterm = (const T*)c->msterm;
+    int rc;
+    if (dir > 0) {
+        // forward: all slices, or a ring with the BDF3 history copied out at
+        // every K-th slice
+        auto at = [&](int s) -> T* { return c->K ? qf_ring<T>(c, s) : (T*)c->qf + (size_t)s * sl; };
+        launch_set_delta<T>(at(0), c->M, c->nr, c->st);  // q(0) = delta_i0
+        c->launches++;
+        for (int s = 1; s <= nmax; ++s) {
+            const int order = s < 3 ? s : 3;
+            if ((rc = contour_step<T>(c, StepKind{order, 1, blk_fwd(c, s)}, at(s - 1), order >= 2 ? at(s - 2) : nullptr,
+                                      order >= 3 ? at(s - 3) : nullptr, at(s), s)))
+                return rc;
+            if (c->K) {
+                const int m = (s + 2) / c->K, j = s + 2 - m * c->K;
+                if (m >= 1 && j <= 2 && m * c->K <= nmax)
+                    CK(cudaMemcpyAsync(qf_ckpt<T>(c, m, j), at(s), sizeof(T) * sl, cudaMemcpyDeviceToDevice, c->st));
+            }
         }
-        int rc = run_step<T>(c, L, lit_c0(order, c->real4), n);
-        if (rc) return rc;
+    } else {
+        const DensityArgs d = density_args(c);
+        const int want_s = c->p.store_qstar == 2 ? 1 : 0;
+        if (c->stream) {
+            CK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, c->st));
+            if (want_s) CK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, c->st));
+            if (c->K && (rc = recompute_segment<T>(c, nmax / c->K))) return rc;
+        }
+        auto slice = [&](int s) -> int {  // streamed density contribution of slice s
+            if (!c->stream) return WLC_OK;
+            launch_density_slice<T>(qf_at<T>(c, s), qb_at<T>(c, s), d, s, want_s, c->jl, c->raw, c->junc, c->qend,
+                                    c->sraw, c->st);
+            c->launches++;
+            return WLC_OK;
+        };
+        launch_set_delta<T>(qb_at<T>(c, nmax), c->M, c->nr, c->st);  // q*(Nmax) = delta_i0
+        c->launches++;
+        slice(nmax);
+        for (int n = 1; n <= nmax; ++n) {
+            const int s = nmax - n;
+            const int order = n < 3 ? n : 3;
+            if ((rc = contour_step<T>(c, StepKind{order, -1, blk_bwd(c, s)}, qb_at<T>(c, s + 1),
+                                      order >= 2 ? qb_at<T>(c, s + 2) : nullptr,
+                                      order >= 3 ? qb_at<T>(c, s + 3) : nullptr, qb_at<T>(c, s), n)))
+                return rc;
+            if (c->K && (s + 1) % c->K == 0 && (rc = recompute_segment<T>(c, s / c->K))) return rc;
+            slice(s);
+        }
     }
     CK(cudaGetLastError());
     if (c->timing) {
@@ -585,6 +778,8 @@ extern "C" int wlc_propagate(wlc_ctx* c, int32_t dir) {
     if (!ready(c)) return WLC_E_STATE;
     if (dir != 1 && dir != -1) return set_err(c, WLC_E_PARAM, "dir must be +1 or -1");
     if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must be called before wlc_propagate");
+    if (dir < 0 && c->stream && !c->have_fwd)
+        return set_err(c, WLC_E_STATE, "with streamed densities (store_qstar 0/2) the forward sweep must come first");
     int rc = c->fp32 ? sweep<float>(c, dir) : sweep<double>(c, dir);
     if (rc) return rc;
     if (dir > 0)
@@ -619,29 +814,26 @@ extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, 
     if (!c->have_fwd || !c->have_bwd)
         return set_err(c, WLC_E_STATE, "both sweeps (wlc_propagate +1 and -1) must precede wlc_density");
     const size_t nr = (size_t)c->nr;
-    DensityArgs d;
-    d.nr = c->nr;
-    d.M = c->M;
-    d.nmax = c->p.nmax;
-    for (int b = 0; b < 3; ++b) {
-        d.nstart[b] = c->nstart[b];
-        d.ns[b] = c->p.ns[b];
-    }
-    d.ds = c->ds;
+    if (s_op && c->p.store_qstar == 0)
+        return set_err(c, WLC_E_STATE, "the orientation tensor is not accumulated with store_qstar = 0 (use 2)");
+    const DensityArgs d = density_args(c);
     S3Args s3;
     for (int a = 0; a < 3; ++a) {
         s3.n[a] = c->N;
         s3.d[a] = c->p.dx[a];
     }
-    if (c->fp32)
-        density_launch<float>(c, d);
-    else
-        density_launch<double>(c, d);
+    if (!c->stream) {  // streamed densities were accumulated by the backward sweep
+        if (c->fp32)
+            density_launch<float>(c, d);
+        else
+            density_launch<double>(c, d);
+    }
     launch_s3(c->qend, 1, 0, s3, c->part, c->scal + 0, c->st);          // S3(q_0(Nmax))
     launch_s3(c->raw, 3, (int64_t)nr, s3, c->part, c->scal + 1, c->st);  // totden
     CK(cudaMemcpyAsync(c->phi, c->raw, sizeof(double) * 3 * nr, cudaMemcpyDeviceToDevice, c->st));
     launch_scale(c->phi, 3 * (int64_t)nr, c->scal + 1, c->vol, c->st);
-    launch_scale(c->junc, 3 * (int64_t)nr, c->scal + 1, c->vol, c->st);
+    CK(cudaMemcpyAsync(c->juncs, c->junc, sizeof(double) * 3 * nr, cudaMemcpyDeviceToDevice, c->st));
+    launch_scale(c->juncs, 3 * (int64_t)nr, c->scal + 1, c->vol, c->st);
     c->launches += 7;
     double hs[2];
     CK(cudaMemcpyAsync(hs, c->scal, sizeof(double) * 2, cudaMemcpyDeviceToHost, c->st));
@@ -651,7 +843,7 @@ extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, 
     int hflag = 0;
     CK(cudaMemcpyAsync(&hflag, c->flag, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     if (phi) CK(cudaMemcpyAsync(phi, c->phi, sizeof(double) * 3 * nr, cudaMemcpyDeviceToHost, c->st));
-    if (junc) CK(cudaMemcpyAsync(junc, c->junc, sizeof(double) * 3 * nr, cudaMemcpyDeviceToHost, c->st));
+    if (junc) CK(cudaMemcpyAsync(junc, c->juncs, sizeof(double) * 3 * nr, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     c->totden = hs[1];
     c->lnq = std::log(hs[0] / c->vol);  // pff_global = ln[(1/V) S3(q_0)], SCFT_Density_FE_ABC.f90:82-92
@@ -659,14 +851,18 @@ extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, 
     if (hflag || !std::isfinite(c->lnq) || !std::isfinite(c->totden))
         return set_err(c, WLC_E_NONFINITE, "non-finite density or partition function");
     if (s_op) {
-        if (c->fp32)
-            stensor_launch<float>(c, d);
-        else
-            stensor_launch<double>(c, d);
-        launch_scale(c->sraw, 15 * (int64_t)nr, c->scal + 1, c->vol, c->st);
-        c->launches += 2;
+        if (!c->stream) {
+            if (c->fp32)
+                stensor_launch<float>(c, d);
+            else
+                stensor_launch<double>(c, d);
+            c->launches++;
+        }
+        CK(cudaMemcpyAsync(c->srs, c->sraw, sizeof(double) * 15 * nr, cudaMemcpyDeviceToDevice, c->st));
+        launch_scale(c->srs, 15 * (int64_t)nr, c->scal + 1, c->vol, c->st);
+        c->launches++;
         std::vector<double> h(15 * nr);
-        CK(cudaMemcpyAsync(h.data(), c->sraw, sizeof(double) * 15 * nr, cudaMemcpyDeviceToHost, c->st));
+        CK(cudaMemcpyAsync(h.data(), c->srs, sizeof(double) * 15 * nr, cudaMemcpyDeviceToHost, c->st));
         CK(cudaStreamSynchronize(c->st));
         // S_OP_blk(r, a, b, blk) at s_op[r + nr*(a + 3b + 9 blk)]; S_zz = -S_xx - S_yy
         for (int b = 0; b < 3; ++b)
@@ -730,6 +926,8 @@ extern "C" int wlc_get_q(wlc_ctx* c, int32_t dir, int32_t s, double* out) {
     if (!ready(c)) return WLC_E_STATE;
     if ((dir != 1 && dir != -1) || s < 0 || s > c->p.nmax || !out)
         return set_err(c, WLC_E_PARAM, "wlc_get_q: bad dir / s / out");
+    if ((dir > 0 && c->K) || (dir < 0 && c->stream))
+        return set_err(c, WLC_E_STATE, "that propagator is not stored (store_qstar / q_checkpoint)");
     return c->fp32 ? get_q<float>(c, dir, s, out) : get_q<double>(c, dir, s, out);
 }
 
@@ -737,6 +935,8 @@ extern "C" int wlc_set_q(wlc_ctx* c, int32_t dir, int32_t s, const double* in) {
     if (!ready(c)) return WLC_E_STATE;
     if ((dir != 1 && dir != -1) || s < 0 || s > c->p.nmax || !in)
         return set_err(c, WLC_E_PARAM, "wlc_set_q: bad dir / s / in");
+    if ((dir > 0 && c->K) || (dir < 0 && c->stream))
+        return set_err(c, WLC_E_STATE, "that propagator is not stored (store_qstar / q_checkpoint)");
     return c->fp32 ? set_q<float>(c, dir, s, in) : set_q<double>(c, dir, s, in);
 }
 
@@ -772,6 +972,8 @@ extern "C" int wlc_init_pr(wlc_ctx* c, int32_t dir, int32_t s, double* pr) {
     if ((dir > 0 && (s < 1 || s > c->p.nmax)) || (dir < 0 && (s < 0 || s > c->p.nmax - 1)))
         return set_err(c, WLC_E_PARAM, "wlc_init_pr: s out of range");
     if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must precede wlc_init_pr");
+    if ((dir > 0 && c->K) || (dir < 0 && c->stream))
+        return set_err(c, WLC_E_STATE, "that propagator is not stored (store_qstar / q_checkpoint)");
     return c->fp32 ? init_pr_impl<float>(c, dir, s, pr) : init_pr_impl<double>(c, dir, s, pr);
 }
 

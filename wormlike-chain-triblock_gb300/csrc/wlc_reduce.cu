@@ -174,6 +174,53 @@ __global__ void stensor_accum(const T* __restrict__ qf, const T* __restrict__ qb
     }
 }
 
+// Streamed form of density_accum / stensor_accum: one slice s per launch,
+// issued by the backward sweep right after q*(s) is computed (descending s),
+// so the q* slices need not be stored.  Same Simpson weights per block.
+template <typename T>
+__global__ void density_slice(const T* __restrict__ a, const T* __restrict__ c, DensityArgs d, int s, int want_s,
+                              JLists jl, double* __restrict__ raw, double* __restrict__ junc,
+                              double* __restrict__ qend, double* __restrict__ sraw) {
+    const int64_t nr = d.nr;
+    double wgt[3];
+    bool any = false;
+    for (int b = 0; b < 3; ++b) {
+        const int j = s - d.nstart[b], n = d.ns[b];
+        wgt[b] = 0.0;
+        if (n > 0 && j >= 0 && j <= n) {
+            wgt[b] = (j == 0 || j == n) ? 1.0 : ((j & 1) ? 4.0 : 2.0);
+            any = true;
+        }
+    }
+    const int sj[3] = {d.nstart[1], d.nstart[2], d.nmax};
+    const bool last = s == 0;
+    const double sc = d.ds / 3.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x) {
+        double sum = 0.0;
+        for (int i = 0; i < d.M; ++i) sum += (double)a[i * nr + r] * (double)c[i * nr + r];
+        if (any)
+            for (int b = 0; b < 3; ++b)
+                if (wgt[b] != 0.0) raw[b * nr + r] += wgt[b] * sum;
+        for (int j = 0; j < 3; ++j)
+            if (s == sj[j]) junc[j * nr + r] = sum;
+        if (s == d.nmax) qend[r] = (double)a[r];
+        if (want_s && any) {
+            for (int t = 0; t < 5; ++t) {
+                double st = 0.0;
+                for (int e = jl.ptr[t]; e < jl.ptr[t + 1]; ++e)
+                    st += jl.val[e] * (double)a[(int64_t)jl.row[e] * nr + r] * (double)c[(int64_t)jl.col[e] * nr + r];
+                for (int b = 0; b < 3; ++b)
+                    if (wgt[b] != 0.0) sraw[((int64_t)b * 5 + t) * nr + r] += wgt[b] * st;
+            }
+        }
+        if (last) {
+            for (int b = 0; b < 3; ++b) raw[b * nr + r] *= sc;
+            if (want_s)
+                for (int q = 0; q < 15; ++q) sraw[(int64_t)q * nr + r] *= sc;
+        }
+    }
+}
+
 // periodic Simpson weight product (utility_mod.f90:236-298): (h/3)*(2|4)
 __device__ __forceinline__ double simpson_w(int64_t r, const S3Args& s) {
     const int x = (int)(r % s.n[0]);
@@ -282,6 +329,12 @@ void launch_stensor(const T* qf, const T* qb, const DensityArgs& d, const JLists
     stensor_accum<T><<<grid_for(d.nr), 128, 0, st>>>(qf, qb, d, jl, sraw);
 }
 
+template <typename T>
+void launch_density_slice(const T* qf_s, const T* qb_s, const DensityArgs& d, int s, int want_s, const JLists& jl,
+                          double* raw, double* junc, double* qend, double* sraw, cudaStream_t st) {
+    density_slice<T><<<grid_for(d.nr), 256, 0, st>>>(qf_s, qb_s, d, s, want_s, jl, raw, junc, qend, sraw);
+}
+
 void launch_s3(const double* a, int nsum, int64_t stride, const S3Args& s, double* part, double* out,
                cudaStream_t st) {
     s3_partial<<<kS3Blocks, 256, 0, st>>>(a, nsum, stride, s, part);
@@ -309,7 +362,9 @@ void launch_nonfinite(const double* a, int64_t n, int* flag, cudaStream_t st) {
                                     double, int, int64_t, T*, cudaStream_t);                                     \
     template void launch_density<T>(const T*, const T*, const DensityArgs&, double*, double*, double*,           \
                                     cudaStream_t);                                                               \
-    template void launch_stensor<T>(const T*, const T*, const DensityArgs&, const JLists&, double*, cudaStream_t);
+    template void launch_stensor<T>(const T*, const T*, const DensityArgs&, const JLists&, double*, cudaStream_t); \
+    template void launch_density_slice<T>(const T*, const T*, const DensityArgs&, int, int, const JLists&, double*, \
+                                          double*, double*, double*, cudaStream_t);
 WLC_INST(double)
 WLC_INST(float)
 #undef WLC_INST

@@ -58,6 +58,12 @@ void launch_density(const T* qf, const T* qb, const DensityArgs& d, double* raw,
                     cudaStream_t st);
 template <typename T>
 void launch_stensor(const T* qf, const T* qb, const DensityArgs& d, const JLists& jl, double* sraw, cudaStream_t st);
+// one contour slice s of the streamed density integrals (q(s), q*(s) given):
+// raw/sraw += Simpson weight x q.q* for the blocks containing s, junction
+// and Q(end) slices copied; at the last slice (s = 0) scaled by ds/3
+template <typename T>
+void launch_density_slice(const T* qf_s, const T* qb_s, const DensityArgs& d, int s, int want_s, const JLists& jl,
+                          double* raw, double* junc, double* qend, double* sraw, cudaStream_t st);
 void launch_s3(const double* a, int nsum, int64_t stride, const S3Args& s, double* part, double* out,
                cudaStream_t st);
 void launch_scale(double* a, int64_t n, const double* denom, double vol, cudaStream_t st);

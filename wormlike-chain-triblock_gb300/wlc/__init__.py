@@ -34,7 +34,8 @@ ERRORS = {-1: "WLC_E_PARAM", -2: "WLC_E_ALLOC", -3: "WLC_E_CUDA", -4: "WLC_E_STA
 SYMBOLS = ["wlc_abi_version", "wlc_create", "wlc_destroy", "wlc_last_error", "wlc_set_box",
            "wlc_set_fields", "wlc_propagate", "wlc_density", "wlc_free_energy", "wlc_get_q",
            "wlc_set_q", "wlc_init_pr", "wlc_mde_one_step", "wlc_launch_count", "wlc_stream",
-           "wlc_enable_timing", "wlc_last_timing", "wlc_iterate", "wlc_reset_mixing", "wlc_get_fields"]
+           "wlc_enable_timing", "wlc_last_timing", "wlc_iterate", "wlc_reset_mixing", "wlc_get_fields",
+           "wlc_set_precision"]
 
 
 class WlcError(RuntimeError):
@@ -48,7 +49,7 @@ class Params(ctypes.Structure):
                 ("ns", ctypes.c_int32 * 3), ("dx", ctypes.c_double * 3), ("loa", ctypes.c_double),
                 ("kappa", ctypes.c_double * 3), ("chi", ctypes.c_double * 3), ("nmu", ctypes.c_double),
                 ("precision", ctypes.c_int32), ("literals", ctypes.c_int32),
-                ("store_qstar", ctypes.c_int32), ("reserved", ctypes.c_int32 * 5)]
+                ("store_qstar", ctypes.c_int32), ("q_checkpoint", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
 
 
 class MixParams(ctypes.Structure):
@@ -111,6 +112,7 @@ def load(build_if_missing=True):
     lib.wlc_iterate.argtypes = [P, ctypes.POINTER(MixParams), Dp, ctypes.POINTER(ctypes.c_int32)]
     lib.wlc_reset_mixing.argtypes = [P]
     lib.wlc_get_fields.argtypes = [P, Dp]
+    lib.wlc_set_precision.argtypes = [P, I]
     _LIB = lib
     return lib
 
@@ -142,7 +144,7 @@ class Instance:
     """One ABC-triblock instance on the current CUDA device."""
 
     def __init__(self, n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_FP64,
-                 literals=WLC_LIT_REAL4):
+                 literals=WLC_LIT_REAL4, store_qstar=1, q_checkpoint=0):
         self.lib = load()
         p = Params()
         n = (n, n, n) if np.isscalar(n) else tuple(n)
@@ -158,7 +160,8 @@ class Instance:
         p.nmu = float(nmu)
         p.precision = int(precision)
         p.literals = int(literals)
-        p.store_qstar = 1
+        p.store_qstar = int(store_qstar)
+        p.q_checkpoint = int(q_checkpoint)
         self.params = p
         self.n = tuple(p.n)
         self.nr = self.n[0] * self.n[1] * self.n[2]
@@ -294,6 +297,11 @@ class Instance:
         conv = ctypes.c_int32(0)
         self._check(self.lib.wlc_iterate(self.h, ctypes.byref(mp), _dp(err), ctypes.byref(conv)))
         return err, bool(conv.value)
+
+    def set_precision(self, precision):
+        """WLC_FP64 or WLC_FP32 propagators from the next sweep on."""
+        self._check(self.lib.wlc_set_precision(self.h, int(precision)))
+        self.params.precision = int(precision)
 
     def reset_mixing(self):
         self._check(self.lib.wlc_reset_mixing(self.h))
