@@ -206,6 +206,42 @@ void* wlc_stream(const wlc_ctx* ctx);
 int wlc_enable_timing(wlc_ctx* ctx, int32_t on);
 int wlc_last_timing(const wlc_ctx* ctx, double* ms4);
 
+/* No counterpart in the reference.  Launch autotuning: time the candidate
+ * launch configurations of one contour step on this context's own data
+ * (pass A variant, threads per solve CTA; all give identical results) and
+ * keep the fastest.  Runs a forward sweep first if none is current.
+ * config (may be NULL) receives {a_variant, solve_threads}.
+ * wlc_set_launch_config sets them by hand (0, 0 = defaults). */
+int wlc_autotune(wlc_ctx* ctx, int32_t* config);
+int wlc_set_launch_config(wlc_ctx* ctx, int32_t a_variant, int32_t solve_threads);
+
+/* No counterpart in the reference (one instance per MPI job there).
+ * Batches: independent FP32 instances (own grid, box, composition, chi,
+ * kappa, Loa, fields; one nmax and lmax; grid edges 16, 24, 32, 40, 48, 64)
+ * advanced together.  One kernel launch per pass per grid-size group per
+ * contour step covers every instance of the group, the streamed density
+ * slices of all instances share one launch per step, and the whole
+ * forward + backward contour loop is captured once as a CUDA graph and
+ * replayed by wlc_batch_propagate.  Each instance is an ordinary context
+ * (wlc_batch_get) for wlc_set_fields, wlc_set_box, wlc_density,
+ * wlc_free_energy, wlc_iterate ...; it shares the batch stream and is
+ * destroyed with the batch only. */
+typedef struct wlc_batch wlc_batch;
+int wlc_batch_create(const wlc_params* p, int32_t count, wlc_batch** out);  /* p[count] */
+int wlc_batch_destroy(wlc_batch* b);
+const char* wlc_batch_last_error(const wlc_batch* b);
+int32_t wlc_batch_size(const wlc_batch* b);
+int32_t wlc_batch_groups(const wlc_batch* b);
+int wlc_batch_get(wlc_batch* b, int32_t i, wlc_ctx** ctx);
+/* MDE_q and MDE_qstar of every instance (wormlike_MDE_2dcomp_mod.f90:231-1557
+ * per instance); the graph is re-captured after a box or Maier-Saupe change. */
+int wlc_batch_propagate(wlc_batch* b);
+/* per grid-size group: config[3g..3g+2] = {N, a_variant, solve_threads} (may be NULL) */
+int wlc_batch_autotune(wlc_batch* b, int32_t* config);
+int wlc_batch_use_graph(wlc_batch* b, int32_t on);  /* 0: issue the launches directly */
+void* wlc_batch_stream(const wlc_batch* b);
+int64_t wlc_batch_launch_count(const wlc_batch* b);
+
 #ifdef __cplusplus
 }
 #endif

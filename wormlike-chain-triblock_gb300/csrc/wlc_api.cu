@@ -57,6 +57,9 @@ struct wlc_ctx {
     void* qb = nullptr;
     int K = 0, nck = 0;
     bool stream = false;
+    bool own_stream = true;   // false: the stream belongs to a batch
+    bool batch_owned = false;
+    int a_variant = 0, solve_threads = 0;  // launch configuration (autotuned or default)
     void* phat = nullptr;
     void* cf = nullptr;
     void* work = nullptr;    // [M][nr] compute type: RHS / one-step scratch
@@ -399,7 +402,7 @@ template <typename T> static int use_precision(wlc_ctx* c) {
     return WLC_OK;
 }
 
-extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
+static int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
     if (!p || !out) return WLC_E_PARAM;
     *out = nullptr;
     wlc_ctx* c = new wlc_ctx();
@@ -431,7 +434,12 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
     *out = c;
     if (!build_basis_tables(c->L, c->real4, c->tab, why)) return set_err(c, WLC_E_SELFTEST, why);
     if ((rc = check_smem(c, c->fp32))) return rc;
-    CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    if (ext) {
+        c->st = ext;
+        c->own_stream = false;
+    } else {
+        CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+    }
     apply_box(c);
     // Theta and J lists
     {
@@ -502,12 +510,22 @@ extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) {
     return WLC_OK;
 }
 
+extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) { return create_impl(p, nullptr, out); }
+
+static int destroy_impl(wlc_ctx* c);
+
 extern "C" int wlc_destroy(wlc_ctx* c) {
+    if (!c) return WLC_OK;
+    if (c->batch_owned) return set_err(c, WLC_E_STATE, "this context belongs to a batch (wlc_batch_destroy)");
+    return destroy_impl(c);
+}
+
+static int destroy_impl(wlc_ctx* c) {
     if (!c) return WLC_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     for (void* p : c->allocs) cudaFree(p);
     for (auto e : c->ev) cudaEventDestroy(e);
-    if (c->st) cudaStreamDestroy(c->st);
+    if (c->st && c->own_stream) cudaStreamDestroy(c->st);
     delete c;
     return WLC_OK;
 }
@@ -533,6 +551,7 @@ extern "C" int wlc_set_box(wlc_ctx* c, double dx, double dy, double dz) {
 
 extern "C" int wlc_set_precision(wlc_ctx* c, int32_t precision) {
     if (!ready(c)) return WLC_E_STATE;
+    if (c->batch_owned) return set_err(c, WLC_E_STATE, "batch instances stay FP32");
     if (precision != WLC_FP64 && precision != WLC_FP32)
         return set_err(c, WLC_E_PARAM, "precision must be WLC_FP64 or WLC_FP32");
     if ((precision == WLC_FP32) == c->fp32) return WLC_OK;
@@ -586,6 +605,8 @@ template <typename T>
 static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h2, const T* h3, T* qout) {
     using C = typename cvec<T>::t;
     StepLaunch<T> L;
+    L.a_variant = c->a_variant;
+    L.solve_threads = c->solve_threads;
     const size_t nr = (size_t)c->nr;
     StepArgs<T>& a = L.step;
     a.h1 = h1;
@@ -1149,3 +1170,485 @@ extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, in
     c->have_fwd = c->have_bwd = c->have_density = false;
     return WLC_OK;
 }
+
+// ------------------------------------------------------------ launch autotuning
+// Candidate launch configurations give bit-identical results (the solve
+// split only changes which thread owns which degree block / m system, and
+// both pass-A variants compute the same sums), so the tuner times them on
+// the instance's own data and keeps the fastest.
+static std::vector<int> solve_thread_candidates(int N) {
+    std::vector<int> out;
+    const int smax = std::max(1, kSolveThreads / N);
+    for (int S : {1, 2, 3, 4, 6, 8, 12, 16})
+        if (S <= smax) out.push_back(N * S);
+    if (out.empty() || out.back() != N * smax) out.push_back(N * smax);
+    return out;
+}
+
+template <typename F> static float time_ms(cudaStream_t st, F&& body, int reps) {
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    body();  // warm-up
+    cudaEventRecord(e0, st);
+    for (int r = 0; r < reps; ++r) body();
+    cudaEventRecord(e1, st);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return ms / (float)reps;
+}
+
+template <typename T> static int autotune_impl(wlc_ctx* c) {
+    int rc;
+    if (!c->have_fwd && (rc = sweep<T>(c, 1))) return rc;
+    c->have_fwd = true;
+    // re-run the last forward step (same inputs, same output) per candidate
+    const size_t sl = (size_t)c->M * c->nr;
+    const int s = c->p.nmax;
+    auto at = [&](int q) -> T* { return c->K ? qf_ring<T>(c, q) : (T*)c->qf + (size_t)q * sl; };
+    StepKind k{3, 1, blk_fwd(c, s)};
+    float best = 1e30f;
+    int best_a = c->a_variant, best_t = c->solve_threads;
+    const bool ms = std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop;
+    for (int av : {1, 2}) {
+        if (av == 2 && sizeof(T) != 4) continue;
+        for (int th : solve_thread_candidates(c->N)) {
+            c->a_variant = av;
+            c->solve_threads = th;
+            StepLaunch<T> L = make_launch<T>(c, k, at(s - 1), at(s - 2), at(s - 3), at(s));
+            if (ms) {  // the Theta term of this step (the buffer holds the last step of the last sweep)
+                launch_ms_term<T>(at(s - 1), at(s - 2), at(s - 3), 3, c->mop, c->thl, c->ds, lit_thresh(c->real4),
+                                  c->M, c->nr, (T*)c->msterm, c->st);
+                L.step.msterm = (const T*)c->msterm;
+            }
+            L.solve.c0 = lit_c0(3, c->real4);
+            const float ms_t = time_ms(c->st, [&] { launch_step<T>(c->N, L, c->st); }, 3);
+            CK(cudaGetLastError());
+            if (ms_t < best) {
+                best = ms_t;
+                best_a = av;
+                best_t = th;
+            }
+        }
+    }
+    c->a_variant = best_a;
+    c->solve_threads = best_t;
+    return WLC_OK;
+}
+
+extern "C" int wlc_autotune(wlc_ctx* c, int32_t* config) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must precede wlc_autotune");
+    int rc = c->fp32 ? autotune_impl<float>(c) : autotune_impl<double>(c);
+    if (rc) return rc;
+    if (config) {
+        config[0] = c->a_variant;
+        config[1] = c->solve_threads;
+    }
+    return WLC_OK;
+}
+
+extern "C" int wlc_set_launch_config(wlc_ctx* c, int32_t a_variant, int32_t solve_threads) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (a_variant < 0 || a_variant > 2 || solve_threads < 0 || solve_threads > kSolveThreads)
+        return set_err(c, WLC_E_PARAM, "a_variant must be 0..2 and solve_threads 0..256");
+    c->a_variant = a_variant;
+    c->solve_threads = solve_threads;
+    return WLC_OK;
+}
+
+// ------------------------------------------------------------ batches
+// Several independent FP32 instances advanced together: one launch per pass
+// per grid-size group per contour step covers every instance of the group
+// (arguments from device arrays, instance = blockIdx.z), the streamed
+// density slices of all instances share one launch per step, and the whole
+// forward + backward contour loop is captured once into a CUDA graph and
+// replayed.
+struct wlc_batch {
+    std::vector<wlc_ctx*> inst;
+    cudaStream_t st = nullptr;
+    std::string err;
+    int nmax = 0, M = 0;
+    struct Group {
+        int N = 0;
+        std::vector<int> idx;
+        StepArgs<float>* dstep = nullptr;  // [2 directions][nmax + 1][count]
+        SolveArgs<float>* dsolve = nullptr;
+        size_t smem = 0;
+        int a_variant = 0, solve_threads = 0;
+    };
+    std::vector<Group> groups;
+    std::vector<int> streamed;                  // instances with streamed densities
+    SliceBatchArgs<float>* dslice = nullptr;    // [streamed]
+    int64_t max_nr_streamed = 0;
+    std::vector<void*> allocs;
+    std::vector<long> sig;  // per instance: box generation and Maier-Saupe state at the last build
+    bool built = false;
+    bool use_graph = true;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t gexec = nullptr;
+    int64_t launches = 0;
+    int64_t per_replay = 0;  // kernel launches in one replay of the graph
+};
+
+static int bset_err(wlc_batch* b, int code, const std::string& msg) {
+    if (b) b->err = msg;
+    return code;
+}
+
+#define BCK(call)                                                                                         \
+    do {                                                                                                  \
+        cudaError_t e_ = (call);                                                                          \
+        if (e_ != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <typename X> static int balloc(wlc_batch* b, X** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        return bset_err(b, WLC_E_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
+    }
+    b->allocs.push_back(q);
+    *p = (X*)q;
+    return WLC_OK;
+}
+
+static void drop_graph(wlc_batch* b) {
+    if (b->gexec) cudaGraphExecDestroy(b->gexec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->gexec = nullptr;
+    b->graph = nullptr;
+}
+
+static bool ms_active(const wlc_ctx* c) { return std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop; }
+
+static std::vector<long> batch_signature(const wlc_batch* b) {
+    std::vector<long> v;
+    for (auto* c : b->inst) v.push_back(2L * c->box_gen + (ms_active(c) ? 1 : 0));
+    return v;
+}
+
+// history / output pointers of step n of direction dir for one instance
+static void step_ptrs(wlc_ctx* c, int dir, int n, const float** h, float** out, StepKind* k) {
+    const size_t sl = (size_t)c->M * c->nr;
+    const int nmax = c->p.nmax;
+    const int s = dir > 0 ? n : nmax - n;
+    const int order = n < 3 ? n : 3;
+    *k = StepKind{order, dir, dir > 0 ? blk_fwd(c, s) : blk_bwd(c, s)};
+    for (int j = 1; j <= 3; ++j) {
+        if (j > order) {
+            h[j - 1] = nullptr;
+            continue;
+        }
+        h[j - 1] = dir > 0 ? (const float*)c->qf + (size_t)(s - j) * sl : qb_at<float>(c, s + j);
+    }
+    *out = dir > 0 ? (float*)c->qf + (size_t)s * sl : qb_at<float>(c, s);
+}
+
+static int batch_build(wlc_batch* b) {
+    const int nmax = b->nmax;
+    for (auto& g : b->groups) {
+        const int cnt = (int)g.idx.size();
+        const size_t tot = (size_t)2 * (nmax + 1) * cnt;
+        std::vector<StepArgs<float>> hs(tot);
+        std::vector<SolveArgs<float>> hv(tot);
+        for (int d = 0; d < 2; ++d)
+            for (int n = 1; n <= nmax; ++n)
+                for (int j = 0; j < cnt; ++j) {
+                    wlc_ctx* c = b->inst[g.idx[j]];
+                    const float* h[3];
+                    float* out;
+                    StepKind k;
+                    step_ptrs(c, d == 0 ? 1 : -1, n, h, &out, &k);
+                    StepLaunch<float> L = make_launch<float>(c, k, h[0], h[1], h[2], out);
+                    L.solve.c0 = lit_c0(k.order, c->real4);
+                    if (ms_active(c)) L.step.msterm = (const float*)c->msterm;
+                    const size_t e = ((size_t)d * (nmax + 1) + n) * cnt + j;
+                    hs[e] = L.step;
+                    hv[e] = L.solve;
+                    const size_t sm = solve_smem_bytes<float>(L.solve);
+                    if (j == 0 && d == 0 && n == 1)
+                        g.smem = sm;
+                    else if (sm != g.smem)
+                        return bset_err(b, WLC_E_UNSUPPORTED, "instances of one grid size need one solve layout");
+                }
+        int rc;
+        if (!g.dstep) {
+            if ((rc = balloc(b, &g.dstep, sizeof(StepArgs<float>) * tot))) return rc;
+            if ((rc = balloc(b, &g.dsolve, sizeof(SolveArgs<float>) * tot))) return rc;
+        }
+        BCK(cudaMemcpy(g.dstep, hs.data(), sizeof(StepArgs<float>) * tot, cudaMemcpyHostToDevice));
+        BCK(cudaMemcpy(g.dsolve, hv.data(), sizeof(SolveArgs<float>) * tot, cudaMemcpyHostToDevice));
+    }
+    if (!b->streamed.empty()) {
+        std::vector<SliceBatchArgs<float>> ha;
+        for (int i : b->streamed) {
+            wlc_ctx* c = b->inst[i];
+            SliceBatchArgs<float> a;
+            a.qf = (const float*)c->qf;
+            a.qb = (const float*)c->qb;
+            a.sl = (int64_t)c->M * c->nr;
+            a.d = density_args(c);
+            a.want_s = c->p.store_qstar == 2 ? 1 : 0;
+            a.jl = c->jl;
+            a.raw = c->raw;
+            a.junc = c->junc;
+            a.qend = c->qend;
+            a.sraw = c->sraw;
+            ha.push_back(a);
+        }
+        int rc;
+        if (!b->dslice && (rc = balloc(b, &b->dslice, sizeof(SliceBatchArgs<float>) * ha.size()))) return rc;
+        BCK(cudaMemcpy(b->dslice, ha.data(), sizeof(SliceBatchArgs<float>) * ha.size(), cudaMemcpyHostToDevice));
+    }
+    b->sig = batch_signature(b);
+    b->built = true;
+    return WLC_OK;
+}
+
+// enqueue the forward and backward sweeps of every instance on the batch stream
+static int batch_issue(wlc_batch* b) {
+    const int nmax = b->nmax;
+    auto step_all = [&](int d, int n) -> int {
+        const int dir = d == 0 ? 1 : -1;
+        for (auto* c : b->inst) {
+            if (!ms_active(c)) continue;
+            const float* h[3];
+            float* out;
+            StepKind k;
+            step_ptrs(c, dir, n, h, &out, &k);
+            launch_ms_term<float>(h[0], h[1], h[2], k.order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M,
+                                  c->nr, (float*)c->msterm, b->st);
+            b->launches++;
+        }
+        for (auto& g : b->groups) {
+            BatchLaunch<float> bl;
+            const int cnt = (int)g.idx.size();
+            const size_t e = ((size_t)d * (nmax + 1) + n) * cnt;
+            bl.dstep = g.dstep + e;
+            bl.dsolve = g.dsolve + e;
+            bl.count = cnt;
+            bl.M = b->M;
+            bl.nkx = g.N / 2 + 1;
+            bl.solve_smem = g.smem;
+            bl.a_variant = g.a_variant;
+            bl.solve_threads = g.solve_threads;
+            cudaError_t err = launch_step_batched(g.N, bl, b->st);
+            b->launches += 3;
+            if (err != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("batched step: ") + cudaGetErrorString(err));
+        }
+        return WLC_OK;
+    };
+    auto slices = [&](int s) {
+        if (b->streamed.empty()) return;
+        launch_density_slice_batched<float>(b->dslice, (int)b->streamed.size(), b->max_nr_streamed, s, b->st);
+        b->launches++;
+    };
+    int rc;
+    for (auto* c : b->inst) {
+        launch_set_delta<float>((float*)c->qf, c->M, c->nr, b->st);
+        b->launches++;
+    }
+    for (int n = 1; n <= nmax; ++n)
+        if ((rc = step_all(0, n))) return rc;
+    for (int i : b->streamed) {
+        wlc_ctx* c = b->inst[i];
+        BCK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, b->st));
+        if (c->p.store_qstar == 2) BCK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, b->st));
+    }
+    for (auto* c : b->inst) {
+        launch_set_delta<float>(qb_at<float>(c, nmax), c->M, c->nr, b->st);
+        b->launches++;
+    }
+    slices(nmax);
+    for (int n = 1; n <= nmax; ++n) {
+        if ((rc = step_all(1, n))) return rc;
+        slices(nmax - n);
+    }
+    BCK(cudaGetLastError());
+    return WLC_OK;
+}
+
+extern "C" int wlc_batch_create(const wlc_params* p, int32_t count, wlc_batch** out) {
+    if (!p || !out || count < 1) return WLC_E_PARAM;
+    wlc_batch* b = new wlc_batch();
+    *out = b;
+    for (int i = 0; i < count; ++i) {
+        const wlc_params& q = p[i];
+        char buf[200];
+        if (q.precision != WLC_FP32 || !supported_batch_n(q.n[0]) || q.q_checkpoint != 0 || q.nmax != p[0].nmax ||
+            q.lmax != p[0].lmax) {
+            std::snprintf(buf, sizeof buf,
+                          "instance %d: batches take FP32 instances with one nmax and lmax, no q_checkpoint, and a "
+                          "grid edge in {16, 24, 32, 40, 48, 64}",
+                          i);
+            return bset_err(b, WLC_E_UNSUPPORTED, buf);
+        }
+    }
+    b->nmax = p[0].nmax;
+    b->M = (p[0].lmax + 1) * (p[0].lmax + 1);
+    BCK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
+    for (int i = 0; i < count; ++i) {
+        wlc_ctx* c = nullptr;
+        int rc = create_impl(&p[i], b->st, &c);
+        if (rc) {
+            b->err = "instance " + std::to_string(i) + ": " + (c ? c->err : std::string("create failed"));
+            if (c) destroy_impl(c);
+            return rc;
+        }
+        c->batch_owned = true;
+        b->inst.push_back(c);
+        bool found = false;
+        for (auto& g : b->groups)
+            if (g.N == c->N) {
+                g.idx.push_back(i);
+                found = true;
+            }
+        if (!found) {
+            wlc_batch::Group g;
+            g.N = c->N;
+            g.idx.push_back(i);
+            b->groups.push_back(g);
+        }
+        if (c->stream) {
+            b->streamed.push_back(i);
+            b->max_nr_streamed = std::max<int64_t>(b->max_nr_streamed, c->nr);
+        }
+    }
+    for (auto& g : b->groups) BCK(prepare_step_batched(g.N));
+    return WLC_OK;
+}
+
+extern "C" int wlc_batch_destroy(wlc_batch* b) {
+    if (!b) return WLC_OK;
+    if (b->st) cudaStreamSynchronize(b->st);
+    drop_graph(b);
+    for (auto* c : b->inst) destroy_impl(c);
+    for (void* q : b->allocs) cudaFree(q);
+    if (b->st) cudaStreamDestroy(b->st);
+    delete b;
+    return WLC_OK;
+}
+
+extern "C" const char* wlc_batch_last_error(const wlc_batch* b) { return b ? b->err.c_str() : "null batch"; }
+
+extern "C" int32_t wlc_batch_size(const wlc_batch* b) { return b ? (int32_t)b->inst.size() : 0; }
+
+extern "C" int wlc_batch_get(wlc_batch* b, int32_t i, wlc_ctx** ctx) {
+    if (!b || !ctx || i < 0 || i >= (int)b->inst.size()) return bset_err(b, WLC_E_PARAM, "bad instance index");
+    *ctx = b->inst[i];
+    return WLC_OK;
+}
+
+extern "C" void* wlc_batch_stream(const wlc_batch* b) { return b ? (void*)b->st : nullptr; }
+
+extern "C" int64_t wlc_batch_launch_count(const wlc_batch* b) { return b ? b->launches : 0; }
+
+extern "C" int wlc_batch_use_graph(wlc_batch* b, int32_t on) {
+    if (!b) return WLC_E_PARAM;
+    b->use_graph = on != 0;
+    drop_graph(b);
+    return WLC_OK;
+}
+
+extern "C" int wlc_batch_propagate(wlc_batch* b) {
+    if (!b || !b->st) return WLC_E_STATE;
+    for (auto* c : b->inst)
+        if (!c->have_fields) return bset_err(b, WLC_E_STATE, "every instance needs wlc_set_fields first");
+    for (auto* c : b->inst)
+        if (c->fp32 == false) return bset_err(b, WLC_E_STATE, "batch instances must stay FP32");
+    int rc;
+    if (!b->built || b->sig != batch_signature(b)) {
+        drop_graph(b);
+        if ((rc = batch_build(b))) return rc;
+    }
+    if (b->use_graph) {
+        if (!b->gexec) {
+            BCK(cudaStreamSynchronize(b->st));
+            BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+            const int64_t l0 = b->launches;
+            rc = batch_issue(b);
+            cudaGraph_t gr = nullptr;
+            cudaError_t e = cudaStreamEndCapture(b->st, &gr);
+            if (rc) {
+                if (gr) cudaGraphDestroy(gr);
+                return rc;
+            }
+            if (e != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+            b->graph = gr;
+            BCK(cudaGraphInstantiate(&b->gexec, b->graph, 0));
+            b->per_replay = b->launches - l0;
+            b->launches = l0;  // counted per replay below
+        }
+        BCK(cudaGraphLaunch(b->gexec, b->st));
+        b->launches += b->per_replay;
+    } else {
+        if ((rc = batch_issue(b))) return rc;
+    }
+    for (auto* c : b->inst) {
+        c->have_fwd = c->have_bwd = true;
+        c->have_density = false;
+    }
+    return WLC_OK;
+}
+
+// Time the batched step of each grid-size group under every candidate
+// launch configuration (on the last forward step, which re-runs with the
+// same inputs and output) and keep the fastest; the graph is re-captured.
+extern "C" int wlc_batch_autotune(wlc_batch* b, int32_t* config) {
+    if (!b || !b->st) return WLC_E_STATE;
+    int rc;
+    if ((rc = wlc_batch_propagate(b))) return rc;
+    const int nmax = b->nmax;
+    for (size_t gi = 0; gi < b->groups.size(); ++gi) {
+        auto& g = b->groups[gi];
+        const int cnt = (int)g.idx.size();
+        float best = 1e30f;
+        int best_a = g.a_variant, best_t = g.solve_threads;
+        for (int av : {1, 2})
+            for (int th : solve_thread_candidates(g.N)) {
+                BatchLaunch<float> bl;
+                const size_t e = (size_t)nmax * cnt;  // direction 0, step nmax
+                bl.dstep = g.dstep + e;
+                bl.dsolve = g.dsolve + e;
+                bl.count = cnt;
+                bl.M = b->M;
+                bl.nkx = g.N / 2 + 1;
+                bl.solve_smem = g.smem;
+                bl.a_variant = av;
+                bl.solve_threads = th;
+                for (int i : g.idx) {  // Theta terms of that step
+                    wlc_ctx* c = b->inst[i];
+                    if (!ms_active(c)) continue;
+                    const float* h[3];
+                    float* out;
+                    StepKind k;
+                    step_ptrs(c, 1, nmax, h, &out, &k);
+                    launch_ms_term<float>(h[0], h[1], h[2], k.order, c->mop, c->thl, c->ds, lit_thresh(c->real4),
+                                          c->M, c->nr, (float*)c->msterm, b->st);
+                }
+                const float t = time_ms(b->st, [&] { launch_step_batched(g.N, bl, b->st); }, 3);
+                BCK(cudaGetLastError());
+                if (t < best) {
+                    best = t;
+                    best_a = av;
+                    best_t = th;
+                }
+            }
+        g.a_variant = best_a;
+        g.solve_threads = best_t;
+        if (config) {
+            config[3 * gi] = g.N;
+            config[3 * gi + 1] = best_a;
+            config[3 * gi + 2] = best_t;
+        }
+    }
+    drop_graph(b);
+    return WLC_OK;
+}
+
+extern "C" int32_t wlc_batch_groups(const wlc_batch* b) { return b ? (int32_t)b->groups.size() : 0; }

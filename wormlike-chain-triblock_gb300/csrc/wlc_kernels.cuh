@@ -122,4 +122,13 @@ __host__ __device__ inline SolveSmem solve_smem(int N, int M, int L, int ndr, in
 
 constexpr int kSolveThreads = 256;  // threads per CTA of the solve kernel (kz x parts in the solve phase)
 
+// Kernel arguments of one launch: the by-value parameter, or (batched
+// launches over several instances) entry blockIdx.z of a device array.
+template <bool B, typename A> __device__ __forceinline__ A pick_args(const A& a0, const A* batch) {
+    if constexpr (B)
+        return batch[blockIdx.z];
+    else
+        return a0;
+}
+
 }  // namespace wlc

@@ -174,13 +174,12 @@ __global__ void stensor_accum(const T* __restrict__ qf, const T* __restrict__ qb
     }
 }
 
-// Streamed form of density_accum / stensor_accum: one slice s per launch,
-// issued by the backward sweep right after q*(s) is computed (descending s),
-// so the q* slices need not be stored.  Same Simpson weights per block.
 template <typename T>
-__global__ void density_slice(const T* __restrict__ a, const T* __restrict__ c, DensityArgs d, int s, int want_s,
-                              JLists jl, double* __restrict__ raw, double* __restrict__ junc,
-                              double* __restrict__ qend, double* __restrict__ sraw) {
+__device__ __forceinline__ void density_slice_body(const T* __restrict__ a, const T* __restrict__ c,
+                                                   const DensityArgs& d, int s, int want_s, const JLists& jl,
+                                                   double* __restrict__ raw, double* __restrict__ junc,
+                                                   double* __restrict__ qend, double* __restrict__ sraw,
+                                                   int64_t r0, int64_t rstep) {
     const int64_t nr = d.nr;
     double wgt[3];
     bool any = false;
@@ -195,7 +194,7 @@ __global__ void density_slice(const T* __restrict__ a, const T* __restrict__ c, 
     const int sj[3] = {d.nstart[1], d.nstart[2], d.nmax};
     const bool last = s == 0;
     const double sc = d.ds / 3.0;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x) {
+    for (int64_t r = r0; r < nr; r += rstep) {
         double sum = 0.0;
         for (int i = 0; i < d.M; ++i) sum += (double)a[i * nr + r] * (double)c[i * nr + r];
         if (any)
@@ -219,6 +218,25 @@ __global__ void density_slice(const T* __restrict__ a, const T* __restrict__ c, 
                 for (int q = 0; q < 15; ++q) sraw[(int64_t)q * nr + r] *= sc;
         }
     }
+}
+
+// Streamed form of density_accum / stensor_accum: one slice s per launch,
+// issued by the backward sweep right after q*(s) is computed (descending s),
+// so the q* slices need not be stored.  Same Simpson weights per block.
+template <typename T>
+__global__ void density_slice(const T* __restrict__ a, const T* __restrict__ c, DensityArgs d, int s, int want_s,
+                              JLists jl, double* __restrict__ raw, double* __restrict__ junc,
+                              double* __restrict__ qend, double* __restrict__ sraw) {
+    density_slice_body<T>(a, c, d, s, want_s, jl, raw, junc, qend, sraw,
+                          blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+}
+
+template <typename T>
+__global__ void density_slice_batched(const SliceBatchArgs<T>* __restrict__ args, int s) {
+    const SliceBatchArgs<T> g = args[blockIdx.y];
+    density_slice_body<T>(g.qf + (int64_t)s * g.sl, g.qb + (int64_t)(s & 3) * g.sl, g.d, s, g.want_s, g.jl, g.raw,
+                          g.junc, g.qend, g.sraw, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
+                          (int64_t)gridDim.x * blockDim.x);
 }
 
 // periodic Simpson weight product (utility_mod.f90:236-298): (h/3)*(2|4)
@@ -335,6 +353,11 @@ void launch_density_slice(const T* qf_s, const T* qb_s, const DensityArgs& d, in
     density_slice<T><<<grid_for(d.nr), 256, 0, st>>>(qf_s, qb_s, d, s, want_s, jl, raw, junc, qend, sraw);
 }
 
+template <typename T>
+void launch_density_slice_batched(const SliceBatchArgs<T>* args, int count, int64_t max_nr, int s, cudaStream_t st) {
+    density_slice_batched<T><<<dim3(grid_for(max_nr), count), 256, 0, st>>>(args, s);
+}
+
 void launch_s3(const double* a, int nsum, int64_t stride, const S3Args& s, double* part, double* out,
                cudaStream_t st) {
     s3_partial<<<kS3Blocks, 256, 0, st>>>(a, nsum, stride, s, part);
@@ -364,7 +387,8 @@ void launch_nonfinite(const double* a, int64_t n, int* flag, cudaStream_t st) {
                                     cudaStream_t);                                                               \
     template void launch_stensor<T>(const T*, const T*, const DensityArgs&, const JLists&, double*, cudaStream_t); \
     template void launch_density_slice<T>(const T*, const T*, const DensityArgs&, int, int, const JLists&, double*, \
-                                          double*, double*, double*, cudaStream_t);
+                                          double*, double*, double*, cudaStream_t);                              \
+    template void launch_density_slice_batched<T>(const SliceBatchArgs<T>*, int, int64_t, int, cudaStream_t);
 WLC_INST(double)
 WLC_INST(float)
 #undef WLC_INST

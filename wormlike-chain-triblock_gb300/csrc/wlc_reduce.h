@@ -61,6 +61,23 @@ void launch_stensor(const T* qf, const T* qb, const DensityArgs& d, const JLists
 // one contour slice s of the streamed density integrals (q(s), q*(s) given):
 // raw/sraw += Simpson weight x q.q* for the blocks containing s, junction
 // and Q(end) slices copied; at the last slice (s = 0) scaled by ds/3
+// per-instance arguments of a batched density_slice launch (instance j =
+// blockIdx.y): q(s) = qf + s*sl, q*(s) = qb + (s & 3)*sl (streamed ring)
+template <typename T> struct SliceBatchArgs {
+    const T* qf;
+    const T* qb;
+    int64_t sl;
+    DensityArgs d;
+    int want_s;
+    JLists jl;
+    double* raw;
+    double* junc;
+    double* qend;
+    double* sraw;
+};
+template <typename T>
+void launch_density_slice_batched(const SliceBatchArgs<T>* args, int count, int64_t max_nr, int s, cudaStream_t st);
+
 template <typename T>
 void launch_density_slice(const T* qf_s, const T* qb_s, const DensityArgs& d, int s, int want_s, const JLists& jl,
                           double* raw, double* junc, double* qend, double* sraw, cudaStream_t st);

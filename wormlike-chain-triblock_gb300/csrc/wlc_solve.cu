@@ -167,8 +167,10 @@ template <typename X> __device__ __forceinline__ void stage(X* dst, const X* src
     for (int e = threadIdx.x; e < n; e += blockDim.x) dst[e] = src[e];
 }
 
-template <typename T, int N>
-__global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1) zfft_solve(SolveArgs<T> a) {
+template <typename T, int N, bool B = false>
+__global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
+    zfft_solve(SolveArgs<T> a0, const SolveArgs<T>* __restrict__ batch) {
+    const SolveArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
     constexpr int NP = N + 1;
     const SolveTablesT<T>& g = a.tab;
@@ -336,22 +338,73 @@ template <typename T> size_t solve_smem_bytes(const SolveArgs<T>& a) {
     return solve_smem(N, a.tab.M, a.tab.L, a.tab.ndr, sizeof(T), a.correct).total;
 }
 
-template <typename T, int N> static cudaError_t launch_solve_n(const SolveArgs<T>& a, cudaStream_t st) {
+// threads per solve CTA: N x S with S parts per kz position (the solve
+// splits each kz system over S threads); 0 = the default kSolveThreads
+template <int N> static int solve_block(int threads) {
+    if (threads <= 0) return kSolveThreads;
+    const int S = threads / N < 1 ? 1 : threads / N;
+    const int b = N * S;
+    return b > kSolveThreads ? (kSolveThreads / N) * N : b;
+}
+
+template <typename T, int N> static cudaError_t launch_solve_n(const SolveArgs<T>& a, cudaStream_t st, int threads) {
     static bool attr_done = false;
     if (!attr_done) {
         cudaFuncSetAttribute(zfft_solve<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
         attr_done = true;
     }
-    zfft_solve<T, N><<<a.nkx * N, kSolveThreads, solve_smem_bytes<T>(a), st>>>(a);
+    zfft_solve<T, N><<<a.nkx * N, solve_block<N>(threads), solve_smem_bytes<T>(a), st>>>(a, nullptr);
     return cudaGetLastError();
 }
 
-template <typename T> cudaError_t launch_solve(int N, const SolveArgs<T>& a, cudaStream_t st) {
+template <typename T> cudaError_t launch_solve(int N, const SolveArgs<T>& a, cudaStream_t st, int threads) {
     switch (N) {
 #define WLC_CASE(n) \
     case n:         \
-        return launch_solve_n<T, n>(a, st);
+        return launch_solve_n<T, n>(a, st, threads);
         WLC_FOR_EACH_N(WLC_CASE)
+#undef WLC_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+template <int N> static cudaError_t set_solve_batched_attr() {
+    static bool attr_done = false;
+    if (!attr_done) {
+        cudaError_t e =
+            cudaFuncSetAttribute(zfft_solve<float, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        if (e != cudaSuccess) return e;
+        attr_done = true;
+    }
+    return cudaSuccess;
+}
+
+template <int N> static cudaError_t launch_solve_batched_n(const BatchLaunch<float>& b, cudaStream_t st) {
+    set_solve_batched_attr<N>();
+    zfft_solve<float, N, true><<<dim3(b.nkx * N, 1, b.count), solve_block<N>(b.solve_threads), b.solve_smem, st>>>(
+        SolveArgs<float>{}, b.dsolve);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_solve_batched(int N, const BatchLaunch<float>& b, cudaStream_t st) {
+    switch (N) {
+#define WLC_CASE(n) \
+    case n:         \
+        return launch_solve_batched_n<n>(b, st);
+        WLC_FOR_EACH_BATCH_N(WLC_CASE)
+#undef WLC_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t prepare_solve_batched(int N) {
+    switch (N) {
+#define WLC_CASE(n) \
+    case n:         \
+        return set_solve_batched_attr<n>();
+        WLC_FOR_EACH_BATCH_N(WLC_CASE)
 #undef WLC_CASE
         default:
             return cudaErrorInvalidValue;
@@ -365,8 +418,8 @@ cudaError_t launch_pivot_table(T* out, int nkeys, int L, double c0, double dcoef
     return cudaGetLastError();
 }
 
-template cudaError_t launch_solve<double>(int, const SolveArgs<double>&, cudaStream_t);
-template cudaError_t launch_solve<float>(int, const SolveArgs<float>&, cudaStream_t);
+template cudaError_t launch_solve<double>(int, const SolveArgs<double>&, cudaStream_t, int);
+template cudaError_t launch_solve<float>(int, const SolveArgs<float>&, cudaStream_t, int);
 template size_t solve_smem_bytes<double>(const SolveArgs<double>&);
 template size_t solve_smem_bytes<float>(const SolveArgs<float>&);
 template cudaError_t launch_pivot_table<double>(double*, int, int, double, double, double, double, const double*,

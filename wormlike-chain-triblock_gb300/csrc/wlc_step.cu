@@ -14,8 +14,29 @@ __device__ __forceinline__ int fold_idx(int i, int n) { return i <= n / 2 ? i : 
 // MDE_ABC.f90:245-375): order 1 (1 - ds w) q1; order 2
 // 2 q1 - q2/2 - ds w (2 q1 - q2); order 3 sum_j c_j(r) q_j with
 // c = (3 - 3 ds w, -3/2 + 3 ds w, 1/3 - ds w) precomputed per block.
+// FP32 form shared by both pass-A kernels (so that they give identical
+// results): dw = ds w(r) rounded once, every operation rounded explicitly.
+__device__ __forceinline__ float rhs_f32(int order, float q1, float q2, float q3, float dw, float third) {
+    if (order == 0) return q1;
+    if (order == 1) return __fmul_rn(__fsub_rn(1.0f, dw), q1);
+    if (order == 2) {
+        const float t = __fsub_rn(__fmul_rn(2.0f, q1), q2);
+        return __fsub_rn(__fsub_rn(__fmul_rn(2.0f, q1), __fmul_rn(0.5f, q2)), __fmul_rn(dw, t));
+    }
+    const float dw3 = __fmul_rn(3.0f, dw);
+    const float c1 = __fsub_rn(3.0f, dw3), c2 = __fadd_rn(-1.5f, dw3), c3 = __fsub_rn(third, dw);
+    return __fmaf_rn(c3, q3, __fmaf_rn(c2, q2, __fmul_rn(c1, q1)));
+}
+
 template <typename T, int NR>
 __device__ __forceinline__ T rhs_value(const StepArgs<T>& a, size_t off, size_t r) {
+    if constexpr (sizeof(T) == 4) {
+        const int o = a.order;
+        float v = rhs_f32(o, a.h1[off], o >= 2 ? a.h2[off] : 0.0f, o >= 3 ? a.h3[off] : 0.0f, o >= 1 ? a.dsw[r] : 0.0f,
+                          a.third);
+        if (a.msterm) v += a.msterm[off];
+        return v;
+    }
     T v;
     if (a.order == 0) {
         v = a.h1[off];
@@ -81,8 +102,9 @@ __device__ __forceinline__ void store_phat(const StepArgs<T>& a, const typename 
 }
 
 // ---------------------------------------------------------------- pass A
-template <typename T, int N>
-__global__ void __launch_bounds__(256) rhs_fft_xy(StepArgs<T> a) {
+template <typename T, int N, bool B = false>
+__global__ void __launch_bounds__(256) rhs_fft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
+    const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
     constexpr int Z = zg_planes(N, sizeof(T));
     constexpr int NR = N * N * N;
@@ -120,18 +142,14 @@ template <int N> struct StagedA {
 __device__ __forceinline__ float rhs_staged(const float* st, int order, size_t P, size_t idx, float third) {
     const float q1 = st[idx];
     if (order == 0) return q1;
-    if (order == 1) return (1.0f - st[P + idx]) * q1;
-    if (order == 2) {
-        const float q2 = st[P + idx], dw = st[2 * P + idx];
-        return 2.0f * q1 - 0.5f * q2 - dw * (2.0f * q1 - q2);
-    }
-    const float q2 = st[P + idx], q3 = st[2 * P + idx], dw = st[3 * P + idx];
-    const float c1 = 3.0f - 3.0f * dw, c2 = -1.5f + 3.0f * dw, c3 = third - dw;
-    return fmaf(c3, q3, fmaf(c2, q2, c1 * q1));
+    if (order == 1) return rhs_f32(1, q1, 0.0f, 0.0f, st[P + idx], third);
+    if (order == 2) return rhs_f32(2, q1, st[P + idx], 0.0f, st[2 * P + idx], third);
+    return rhs_f32(3, q1, st[P + idx], st[2 * P + idx], st[3 * P + idx], third);
 }
 
-template <int N>
-__global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a) {
+template <int N, bool B = false>
+__global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, const StepArgs<float>* __restrict__ batch) {
+    const StepArgs<float> a = pick_args<B>(a0, batch);
     using C = float2;
     constexpr int Z = StagedA<N>::Z;
     constexpr int NKX = N / 2 + 1;
@@ -190,8 +208,9 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a) {
 }
 
 // ---------------------------------------------------------------- pass C
-template <typename T, int N>
-__global__ void __launch_bounds__(256) ifft_xy(StepArgs<T> a) {
+template <typename T, int N, bool B = false>
+__global__ void __launch_bounds__(256) ifft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
+    const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
     constexpr int Z = zg_planes(N, sizeof(T));
     constexpr int NKX = N / 2 + 1;
@@ -266,32 +285,88 @@ template <typename T> size_t smem_xy(int N) {
     return sizeof(C) * ((size_t)N + (size_t)(N / 2) * N + (size_t)zg_planes(N, sizeof(T)) * N * (N / 2 + 1));
 }
 
+template <typename T, int N, bool B> static void set_xy_attrs() {
+    static bool done = false;
+    if (done) return;
+    cudaFuncSetAttribute(rhs_fft_xy<T, N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(ifft_xy<T, N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
+        cudaFuncSetAttribute(rhs_fft_xy_staged<N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)StagedA<N>::bytes);
+    done = true;
+}
+
+// pass A variant: 0 = default (staged where it fits), 1 = generic, 2 = staged
+template <typename T, int N> static bool use_staged(int variant) {
+    if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
+        return variant != 1;
+    else
+        return false;
+}
+
 template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s, cudaStream_t st) {
     constexpr int Z = zg_planes(N, sizeof(T));
     const size_t sxy = smem_xy<T>(N);
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaFuncSetAttribute(rhs_fft_xy<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(ifft_xy<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
-            cudaFuncSetAttribute(rhs_fft_xy_staged<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)StagedA<N>::bytes);
-        attr_done = true;
-    }
+    set_xy_attrs<T, N, false>();
     const dim3 gxy(N / Z, s.step.M);
     if (s.events) cudaEventRecord(s.events[0], st);
     if (s.do_a) {
-        if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
-            rhs_fft_xy_staged<N><<<gxy, 512, StagedA<N>::bytes, st>>>(s.step);
-        else
-            rhs_fft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step);
+        bool staged = false;
+        if constexpr (sizeof(T) == 4 && StagedA<N>::fits) {
+            staged = use_staged<T, N>(s.a_variant);
+            if (staged) rhs_fft_xy_staged<N><<<gxy, 512, StagedA<N>::bytes, st>>>(s.step, nullptr);
+        }
+        if (!staged) rhs_fft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step, nullptr);
     }
     if (s.events) cudaEventRecord(s.events[1], st);
-    if (s.do_b) launch_solve<T>(N, s.solve, st);
+    if (s.do_b) launch_solve<T>(N, s.solve, st, s.solve_threads);
     if (s.events) cudaEventRecord(s.events[2], st);
-    if (s.do_c) ifft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step);
+    if (s.do_c) ifft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step, nullptr);
     if (s.events) cudaEventRecord(s.events[3], st);
     return cudaGetLastError();
+}
+
+template <int N> static cudaError_t launch_batched_n(const BatchLaunch<float>& b, cudaStream_t st) {
+    constexpr int Z = zg_planes(N, 4);
+    const size_t sxy = smem_xy<float>(N);
+    set_xy_attrs<float, N, true>();
+    const dim3 gxy(N / Z, b.M, b.count);
+    bool staged = false;
+    if constexpr (StagedA<N>::fits) {
+        staged = use_staged<float, N>(b.a_variant);
+        if (staged) rhs_fft_xy_staged<N, true><<<gxy, 512, StagedA<N>::bytes, st>>>(StepArgs<float>{}, b.dstep);
+    }
+    if (!staged) rhs_fft_xy<float, N, true><<<gxy, 256, sxy, st>>>(StepArgs<float>{}, b.dstep);
+    cudaError_t e = launch_solve_batched(N, b, st);
+    if (e != cudaSuccess) return e;
+    ifft_xy<float, N, true><<<gxy, 256, sxy, st>>>(StepArgs<float>{}, b.dstep);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_step_batched(int N, const BatchLaunch<float>& b, cudaStream_t st) {
+    switch (N) {
+#define WLC_CASE(n) \
+    case n:         \
+        return launch_batched_n<n>(b, st);
+        WLC_FOR_EACH_BATCH_N(WLC_CASE)
+#undef WLC_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
+}
+
+// function attributes of the batched kernels, set outside any stream capture
+cudaError_t prepare_step_batched(int N) {
+    switch (N) {
+#define WLC_CASE(n)                          \
+    case n:                                  \
+        set_xy_attrs<float, n, true>();      \
+        return prepare_solve_batched(n);
+        WLC_FOR_EACH_BATCH_N(WLC_CASE)
+#undef WLC_CASE
+        default:
+            return cudaErrorInvalidValue;
+    }
 }
 
 template <typename T> cudaError_t launch_step(int N, const StepLaunch<T>& s, cudaStream_t st) {

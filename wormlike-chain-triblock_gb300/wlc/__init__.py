@@ -35,7 +35,10 @@ SYMBOLS = ["wlc_abi_version", "wlc_create", "wlc_destroy", "wlc_last_error", "wl
            "wlc_set_fields", "wlc_propagate", "wlc_density", "wlc_free_energy", "wlc_get_q",
            "wlc_set_q", "wlc_init_pr", "wlc_mde_one_step", "wlc_launch_count", "wlc_stream",
            "wlc_enable_timing", "wlc_last_timing", "wlc_iterate", "wlc_reset_mixing", "wlc_get_fields",
-           "wlc_set_precision"]
+           "wlc_set_precision", "wlc_autotune", "wlc_set_launch_config", "wlc_batch_create",
+           "wlc_batch_destroy", "wlc_batch_last_error", "wlc_batch_size", "wlc_batch_groups", "wlc_batch_get",
+           "wlc_batch_propagate", "wlc_batch_autotune", "wlc_batch_use_graph", "wlc_batch_stream",
+           "wlc_batch_launch_count"]
 
 
 class WlcError(RuntimeError):
@@ -113,6 +116,23 @@ def load(build_if_missing=True):
     lib.wlc_reset_mixing.argtypes = [P]
     lib.wlc_get_fields.argtypes = [P, Dp]
     lib.wlc_set_precision.argtypes = [P, I]
+    Ip = ctypes.POINTER(ctypes.c_int32)
+    lib.wlc_autotune.argtypes = [P, Ip]
+    lib.wlc_set_launch_config.argtypes = [P, I, I]
+    lib.wlc_batch_create.argtypes = [ctypes.POINTER(Params), I, ctypes.POINTER(P)]
+    lib.wlc_batch_destroy.argtypes = [P]
+    lib.wlc_batch_last_error.argtypes = [P]
+    lib.wlc_batch_last_error.restype = ctypes.c_char_p
+    lib.wlc_batch_size.argtypes = [P]
+    lib.wlc_batch_groups.argtypes = [P]
+    lib.wlc_batch_get.argtypes = [P, I, ctypes.POINTER(P)]
+    lib.wlc_batch_propagate.argtypes = [P]
+    lib.wlc_batch_autotune.argtypes = [P, Ip]
+    lib.wlc_batch_use_graph.argtypes = [P, I]
+    lib.wlc_batch_stream.argtypes = [P]
+    lib.wlc_batch_stream.restype = P
+    lib.wlc_batch_launch_count.argtypes = [P]
+    lib.wlc_batch_launch_count.restype = ctypes.c_int64
     _LIB = lib
     return lib
 
@@ -140,33 +160,37 @@ def wlc_radius_of_gyration(x):
     return math.sqrt(1.0 / (3.0 * x) - 1.0 / x ** 2 + 2.0 / x ** 3 - 2.0 / x ** 4 * (1.0 - math.exp(-x)))
 
 
+def make_params(n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_FP64, literals=WLC_LIT_REAL4,
+                store_qstar=1, q_checkpoint=0):
+    """wlc_params of one instance (kappa, chi: 3-tuples; n, dx: scalar or 3-tuple)."""
+    p = Params()
+    n = (n, n, n) if np.isscalar(n) else tuple(n)
+    dx = (dx, dx, dx) if np.isscalar(dx) else tuple(dx)
+    p.n[:] = [int(v) for v in n]
+    p.lmax = int(lmax)
+    p.nmax = int(nmax)
+    p.ns[:] = [int(v) for v in ns]
+    p.dx[:] = [float(v) for v in dx]
+    p.loa = float(loa)
+    p.kappa[:] = [float(v) for v in kappa]
+    p.chi[:] = [float(v) for v in chi]
+    p.nmu = float(nmu)
+    p.precision = int(precision)
+    p.literals = int(literals)
+    p.store_qstar = int(store_qstar)
+    p.q_checkpoint = int(q_checkpoint)
+    return p
+
+
 class Instance:
     """One ABC-triblock instance on the current CUDA device."""
 
     def __init__(self, n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_FP64,
                  literals=WLC_LIT_REAL4, store_qstar=1, q_checkpoint=0):
         self.lib = load()
-        p = Params()
-        n = (n, n, n) if np.isscalar(n) else tuple(n)
-        dx = (dx, dx, dx) if np.isscalar(dx) else tuple(dx)
-        p.n[:] = [int(v) for v in n]
-        p.lmax = int(lmax)
-        p.nmax = int(nmax)
-        p.ns[:] = [int(v) for v in ns]
-        p.dx[:] = [float(v) for v in dx]
-        p.loa = float(loa)
-        p.kappa[:] = [float(v) for v in kappa]
-        p.chi[:] = [float(v) for v in chi]
-        p.nmu = float(nmu)
-        p.precision = int(precision)
-        p.literals = int(literals)
-        p.store_qstar = int(store_qstar)
-        p.q_checkpoint = int(q_checkpoint)
-        self.params = p
-        self.n = tuple(p.n)
-        self.nr = self.n[0] * self.n[1] * self.n[2]
-        self.M = (p.lmax + 1) ** 2
-        self.nmax = p.nmax
+        p = make_params(n, lmax, nmax, ns, dx, loa, kappa, chi, nmu, precision, literals, store_qstar, q_checkpoint)
+        self._init_from(p)
+        self.owned = True
         self.h = ctypes.c_void_p()
         rc = self.lib.wlc_create(ctypes.byref(p), ctypes.byref(self.h))
         if rc != 0:
@@ -175,14 +199,32 @@ class Instance:
             self.h = None
             raise WlcError(rc, msg)
 
+    def _init_from(self, p):
+        self.params = p
+        self.n = tuple(p.n)
+        self.nr = self.n[0] * self.n[1] * self.n[2]
+        self.M = (p.lmax + 1) ** 2
+        self.nmax = p.nmax
+
+    @classmethod
+    def _wrap(cls, lib, h, p, owner):
+        """A batch member: the handle belongs to the batch (owner)."""
+        self = cls.__new__(cls)
+        self.lib = lib
+        self._init_from(p)
+        self.owned = False
+        self.h = h
+        self._owner = owner
+        return self
+
     def _check(self, rc):
         if rc != 0:
             raise WlcError(rc, self.lib.wlc_last_error(self.h).decode())
 
     def close(self):
-        if getattr(self, "h", None):
+        if getattr(self, "h", None) and getattr(self, "owned", True):
             self.lib.wlc_destroy(self.h)
-            self.h = None
+        self.h = None
 
     def __del__(self):
         try:
@@ -303,6 +345,16 @@ class Instance:
         self._check(self.lib.wlc_set_precision(self.h, int(precision)))
         self.params.precision = int(precision)
 
+    def autotune(self):
+        """Time the launch configurations of a contour step on this
+        instance's data and keep the fastest; returns (a_variant, solve_threads)."""
+        cfg = (ctypes.c_int32 * 2)()
+        self._check(self.lib.wlc_autotune(self.h, cfg))
+        return int(cfg[0]), int(cfg[1])
+
+    def set_launch_config(self, a_variant=0, solve_threads=0):
+        self._check(self.lib.wlc_set_launch_config(self.h, int(a_variant), int(solve_threads)))
+
     def reset_mixing(self):
         self._check(self.lib.wlc_reset_mixing(self.h))
 
@@ -330,3 +382,75 @@ class Instance:
             if callback is not None:
                 callback(n, fe, err)
         return dict(F=fe, lnQ=d["lnQ"] if d else float("nan"), n_iter=n, converged=conv, history=hist)
+
+
+class Batch:
+    """Independent FP32 instances advanced together (wlc_batch_*): batched
+    launches per grid-size group, the contour loop replayed as a CUDA graph.
+    `specs` is a list of make_params keyword dicts; members are Instance
+    objects (self.instances) for fields, densities, free energy and mixing."""
+
+    def __init__(self, specs):
+        self.lib = load()
+        arr = (Params * len(specs))()
+        for i, kw in enumerate(specs):
+            kw = dict(kw)
+            kw.setdefault("precision", WLC_FP32)
+            kw.setdefault("store_qstar", 0)
+            arr[i] = make_params(**kw)
+        self.h = ctypes.c_void_p()
+        rc = self.lib.wlc_batch_create(arr, len(specs), ctypes.byref(self.h))
+        if rc != 0:
+            msg = self.lib.wlc_batch_last_error(self.h).decode() if self.h else ""
+            self.lib.wlc_batch_destroy(self.h)
+            self.h = None
+            raise WlcError(rc, msg)
+        self.instances = []
+        for i in range(len(specs)):
+            hi = ctypes.c_void_p()
+            self._check(self.lib.wlc_batch_get(self.h, i, ctypes.byref(hi)))
+            self.instances.append(Instance._wrap(self.lib, hi, arr[i], self))
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WlcError(rc, self.lib.wlc_batch_last_error(self.h).decode())
+
+    def __len__(self):
+        return len(self.instances)
+
+    def __getitem__(self, i):
+        return self.instances[i]
+
+    def propagate(self):
+        """MDE_q and MDE_qstar of every instance."""
+        self._check(self.lib.wlc_batch_propagate(self.h))
+
+    def autotune(self):
+        g = self.lib.wlc_batch_groups(self.h)
+        cfg = (ctypes.c_int32 * (3 * max(1, g)))()
+        self._check(self.lib.wlc_batch_autotune(self.h, cfg))
+        return [(int(cfg[3 * i]), int(cfg[3 * i + 1]), int(cfg[3 * i + 2])) for i in range(g)]
+
+    def use_graph(self, on=True):
+        self._check(self.lib.wlc_batch_use_graph(self.h, 1 if on else 0))
+
+    @property
+    def stream(self):
+        return self.lib.wlc_batch_stream(self.h)
+
+    @property
+    def launch_count(self):
+        return self.lib.wlc_batch_launch_count(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for inst in getattr(self, "instances", []):
+                inst.h = None
+            self.lib.wlc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
