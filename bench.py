@@ -215,6 +215,7 @@ def run_ours(args, wl):
                         precision=wlc.WLC_FP64 if wl["precision"] == "fp64" else wlc.WLC_FP32)
     nr = wl["n"] ** 3
     rng = np.random.default_rng(1234 + rank)
+    tuned = None
     w_host = torch.empty((3, nr), dtype=torch.float64).pin_memory()
     w_host.numpy()[:] = rng.normal(0.0, wl["w_sigma"], size=(3, nr))
     phi_host = torch.empty((3, nr), dtype=torch.float64).pin_memory()
@@ -252,6 +253,8 @@ def run_ours(args, wl):
             torch.cuda.synchronize()
 
     check(lib.wlc_set_fields(h, wp, None))
+    if not args.no_autotune:
+        tuned = inst.autotune()
     for _ in range(args.warmup):
         device_step()
     barrier()
@@ -335,7 +338,8 @@ def run_ours(args, wl):
                                        "L/lp=2.0; one bench step = forward + backward sweep + densities "
                                        "(400 contour steps)",
                            "precision": wl["precision"], "l2": "inputs larger than L2 (51 GB history/direction)",
-                           "parallelism": "replicas" if world > 1 else "single"},
+                           "parallelism": "replicas" if world > 1 else "single",
+                           "launch_config": {"a_variant": tuned[0], "solve_threads": tuned[1]} if tuned else "default"},
                 "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "wall_s": t_wall}
@@ -355,6 +359,9 @@ def run_profile_case(args):
                         precision=wlc.WLC_FP64 if args.precision == "fp64" else wlc.WLC_FP32)
     rng = np.random.default_rng(5)
     inst.set_fields(rng.normal(0.0, wl["w_sigma"], size=(3, wl["n"] ** 3)))
+    if args.launch_config:
+        a_var, threads = (int(v) for v in args.launch_config.split(","))
+        inst.set_launch_config(a_var, threads)
     inst.MDE_q()
     inst.MDE_q()
     inst.MDE_qstar()
@@ -429,6 +436,102 @@ def run_converge(args):
     print(json.dumps(out))
 
 
+def batch_specs(count=48, seed=3):
+    """The batched sweep workload: `count` independent instances, grid edge
+    drawn from {24, 32, 40, 48}, l <= 8, Ns = 128, fA, fC ~ U(0.2, 0.4),
+    fB = 1 - fA - fC, chiN ~ U(12, 24) for all pairs, contour/persistence
+    ~ U(0.5, 3.0), box edge 5.0 Rg; FP32 propagators, streamed densities."""
+    import wlc
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(count):
+        n = int(rng.choice([24, 32, 40, 48]))
+        fa, fc = rng.uniform(0.2, 0.4), rng.uniform(0.2, 0.4)
+        chi = float(rng.uniform(12.0, 24.0))
+        x = float(rng.uniform(0.5, 3.0))
+        box = 5.0 * wlc.wlc_radius_of_gyration(x)
+        specs.append(dict(n=n, lmax=8, nmax=128, ns=wlc.even_block_lengths((fa, 1.0 - fa - fc, fc), 128),
+                          dx=box / n, loa=x * 0.5, kappa=(0.5, 0.5, 0.5), chi=(chi, chi, chi),
+                          precision=wlc.WLC_FP32, store_qstar=0, seed=1000 + i))
+    return specs
+
+
+def run_batch(args):
+    """Batched sweep: all instances' forward + backward sweeps per bench
+    step (one graph replay), against the same instances swept one by one."""
+    import torch
+    import wlc
+    specs = batch_specs(args.count)
+    seeds = [s.pop("seed") for s in specs]
+    b = wlc.Batch(specs)
+    for inst, spec, sd in zip(b.instances, specs, seeds):
+        inst.set_fields(np.random.default_rng(sd).normal(0.0, 0.3, size=(3, spec["n"] ** 3)))
+    stream = torch.cuda.ExternalStream(b.stream)
+    cfg = None if args.no_autotune else b.autotune()
+    for _ in range(args.warmup):
+        b.propagate()
+    torch.cuda.synchronize()
+    clk = ClockSampler(0)
+    clk.start()
+    l0 = b.launch_count
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.propagate()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = b.launch_count - l0
+    steps = 2 * 128 * len(specs) * args.steps
+    value = steps / (ms / 1000.0)
+    # the same instances swept one by one (no batching, no graph)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        for inst in b.instances:
+            inst.MDE_q()
+            inst.MDE_qstar()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = ev0.elapsed_time(ev1)
+    # end to end: fields in from the host, densities and free energies out
+    w_host = [np.random.default_rng(sd).normal(0.0, 0.3, size=(3, sp["n"] ** 3)) for sp, sd in zip(specs, seeds)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        for inst, w in zip(b.instances, w_host):
+            inst.set_fields(w)
+            h2d += w.nbytes
+        b.propagate()
+        for inst in b.instances:
+            d = inst.density(want_junction=False)
+            inst.free_energy()
+            d2h += d["phi"].nbytes + 16
+    torch.cuda.synchronize()
+    e2e = steps / (time.perf_counter() - t0)
+    groups = {}
+    for sp in specs:
+        groups[sp["n"]] = groups.get(sp["n"], 0) + 1
+    line = {"metric": "MDE contour steps/s, %d batched ABC instances (l<=8, Ns=128)" % len(specs),
+            "value": value, "unit": "steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (per-instance seeded N(0,0.3^2) fields)",
+            "config": {"workload": "%d instances, N in {24,32,40,48} (%s), L=8, Ns=128, fA,fC~U(.2,.4), "
+                                   "chiN~U(12,24), L/lp~U(.5,3), box 5 Rg; FP32 propagators, streamed densities; one "
+                                   "bench step = forward + backward sweep of every instance" % (
+                                       len(specs), ", ".join("%d x %d^3" % (v, k) for k, v in sorted(groups.items()))),
+                       "l2": "inputs larger than L2 (the stored forward propagators total ~110 GB)",
+                       "autotuned": cfg},
+            "unbatched": {"value": steps / (ms_seq / 1000.0), "unit": "steps/s",
+                          "note": "same instances swept one after another, one launch per pass per instance"},
+            "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps},
+            "gpu_launches": int(launches), "clocks": clocks}
+    print(json.dumps(line))
+    b.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -439,6 +542,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="small-footprint case for ncu captures")
     ap.add_argument("--converge", action="store_true", help="time-to-converged F instead of steps/s")
+    ap.add_argument("--workload", default="single", choices=["single", "batch"])
+    ap.add_argument("--count", type=int, default=48, help="instances of the batched workload")
+    ap.add_argument("--no-autotune", action="store_true", help="default launch configuration")
+    ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads")
     ap.add_argument("--forms", default="fp32sched,fp64")
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--switch-tol", type=float, default=1e-4)
@@ -454,6 +561,9 @@ def main():
         return
     if args.converge:
         run_converge(args)
+        return
+    if args.workload == "batch" and args.impl == "ours":
+        run_batch(args)
         return
     wl = workload(args.precision)
     if args.impl == "reference":
