@@ -39,7 +39,8 @@ enum {
     WLC_E_STATE = -4,     /* call order violated (e.g. density before sweeps)   */
     WLC_E_NONFINITE = -5, /* NaN/Inf detected in a result                       */
     WLC_E_UNSUPPORTED = -6, /* size/option combination not built                */
-    WLC_E_SELFTEST = -7   /* host-side consistency check of the G(k) factorisation failed */
+    WLC_E_SELFTEST = -7,  /* host-side consistency check of the G(k) factorisation failed */
+    WLC_E_IO = -8         /* a file could not be opened, written or parsed          */
 };
 
 enum { WLC_FP64 = 0, WLC_FP32 = 1 };
@@ -128,10 +129,11 @@ typedef struct wlc_mix_params {
     int32_t min_iter;         /* 20: converged stays 0 while n_iter < min_iter             */
     int32_t relax_iter;       /* 150: from this n_iter on (nmu == 0 only) ...              */
     double relax_tol;         /* ... 5e-4 is enough; relax_iter <= 0 disables it           */
-    int32_t reserved[4];
+    double lambda_m;          /* lanbtM = 0.08: Maier-Saupe tensor mixing (nmu != 0)       */
+    int32_t reserved[2];
 } wlc_mix_params;
 
-/* iterate(converge) (AB_iterate, SCFT_iterate.f90:27-334, three-block
+/* iterate(converge) (AB_iterate, SCFT_iterate.f90:27-522, three-block
  * form): from the last wlc_density result, update the fields on the device
  * by simple mixing (n_iter <= num_simple) or Anderson mixing (least squares
  * in FP64 on the device).  With f_J = N_J/Nmax, the simple-mixing residual is
@@ -140,7 +142,11 @@ typedef struct wlc_mix_params {
  * (both reduce to the reference's two-block formulas).
  * err[0..2]: block errors (max |dW_K| while simple mixing,
  * sqrt(<dW_K,dW_K>/<w_K^out,w_K^out>) with Anderson; global, not a mean of
- * per-rank maxima); err[3]: incompressibility residual max |sum_K phi_K - 1|.
+ * per-rank maxima); err[3]: incompressibility residual max |sum_K phi_K - 1|;
+ * err[4]: with nmu != 0, tm_diff = max |NMu S - M| before the Maier-Saupe
+ * update M += lambda_m (NMu S - M) (S summed over the blocks; 0 otherwise),
+ * and convergence also needs err[4] < 5 tol (SCFT_iterate.f90:1124-1139).
+ * err has 5 entries.
  * n_iter counts the calls since creation, the last wlc_reset_mixing or a
  * change of anderson_depth.  The fields of the next wlc_propagate are the
  * updated ones; wlc_get_fields reads them. */
@@ -149,6 +155,9 @@ int wlc_reset_mixing(wlc_ctx* ctx);
 
 /* Copy the current fields W_blk(0:LS,1:3) to the host (w[blk*nr + r]). */
 int wlc_get_fields(wlc_ctx* ctx, double* w);
+/* Copy the current Maier-Saupe tensor M_OP(0:LS,0:2,0:2) to the host
+ * (m_op[r + nr*(a + 3*b)], the layout of wlc_set_fields). */
+int wlc_get_mop(wlc_ctx* ctx, double* m_op);
 
 /* No counterpart in the reference (which is FP64 only).  Switch the
  * propagator precision of an existing context between WLC_FP64 and WLC_FP32
@@ -241,6 +250,28 @@ int wlc_batch_autotune(wlc_batch* b, int32_t* config);
 int wlc_batch_use_graph(wlc_batch* b, int32_t on);  /* 0: issue the launches directly */
 void* wlc_batch_stream(const wlc_batch* b);
 int64_t wlc_batch_launch_count(const wlc_batch* b);
+
+/* The reference's files (host arrays only, no context needed), for
+ * starting from the Fortran code's output and the other way round.
+ *  W<rank>.dat: "K W_A W_B W_C" per grid point (W_dump, SCFT_dump.f90:296-300);
+ *    wlc_io_read_w also takes the two-block "K W_A W_B" form (readW,
+ *    init_array_2dcomp_mod.f90:1088-1093), with w_C = 0.  w[blk*nr + r].
+ *  M_OP<rank>.dat: three lines "Lx Ly Lz M(a,0) M(a,1) M(a,2)" per point
+ *    (SCFT_dump.f90:302-308); m_op[r + nr*(a + 3*b)], box = {Lx, Ly, Lz}.
+ *  RHO_total.dat: '(3f10.6,3f12.8)' x y z phi_A phi_B phi_C, z outermost
+ *    (SCFT_dump.f90:116-127); phi[blk*nr + r].
+ *  FreeEG.dat: "n_iter F lnQ F+lnQ F-F_FH" and "n_iter box FE-FH F-F_FH"
+ *    (SCFT_dump.f90:40-42), F_FH = sum_{K<J} chi_KJ f_K f_J; chi = (AB, AC, BC).
+ *  error.dat: "n_iter err..." (SCFT_dump.f90:36-38).
+ * Return WLC_E_IO when a file cannot be opened, written or parsed. */
+int wlc_io_write_w(const char* path, const double* w, int64_t nr);
+int wlc_io_read_w(const char* path, double* w, int64_t nr);
+int wlc_io_write_mop(const char* path, const double* m_op, int64_t nr, const double* box);
+int wlc_io_read_mop(const char* path, double* m_op, int64_t nr);
+int wlc_io_write_rho(const char* path, const double* phi, const int32_t* n, const double* dx);
+int wlc_io_append_free_energy(const char* path, int32_t n_iter, double fe, double lnq, double box,
+                              const double* chi, const int32_t* ns, int32_t nmax);
+int wlc_io_append_errors(const char* path, int32_t n_iter, const double* err, int32_t nerr);
 
 #ifdef __cplusplus
 }

@@ -16,7 +16,10 @@ interaction matrix):
   * U_mn = <dW_k - dW_km, dW_k - dW_kn>, V_m = <dW_k - dW_km, dW_k> summed
     over the blocks (:237-276), U c = V by LU (dgetrf/dgetrs,
     matrix_inverse_mod.f90:167-199), new w from :307-331;
-  * convergence (:1124-1160): every block error < CC, or (nmu == 0,
+  * Maier-Saupe tensor (nmu != 0) by simple mixing (:351-372),
+    M += lanbtM (NMu S - M), S summed over the blocks;
+  * convergence (:1124-1160): every block error < CC (and the M error
+    < 5 CC when nmu != 0), or (nmu == 0,
     n_iter >= 150) every error < 5e-4; never while n_iter < 20
     (SCFT_control.f90:270-272);
   * <a, b> = S3(a b)/V (dot_product_mpi, :1193-1237).
@@ -63,7 +66,8 @@ def lu_solve(U, V):
 
 class Mixer:
     def __init__(self, oracle_instance, chi, ns, nmax, depth=5, num_simple=20, lambda_simple=0.1,
-                 lambda_anderson=0.1, tol=1e-4, min_iter=20, relax_iter=150, relax_tol=5e-4, nmu=0.0):
+                 lambda_anderson=0.1, tol=1e-4, min_iter=20, relax_iter=150, relax_tol=5e-4, nmu=0.0,
+                 lambda_m=0.08):
         self.o = oracle_instance
         self.C = np.array([[0.0, chi[0], chi[1]], [chi[0], 0.0, chi[2]], [chi[1], chi[2], 0.0]])
         self.f = np.array(ns, dtype=np.float64) / float(nmax)
@@ -72,6 +76,8 @@ class Mixer:
         self.depth, self.ns = depth, num_simple
         self.ls, self.la, self.tol, self.min_iter = lambda_simple, lambda_anderson, tol, min_iter
         self.relax_iter, self.relax_tol, self.nmu = relax_iter, relax_tol, nmu
+        self.lambda_m = lambda_m
+        self.mop = None  # Maier-Saupe tensor after the last step (nmu != 0)
         self.n = 0
         nr = oracle_instance.nr
         self.wout = np.zeros((depth + 1, 3, nr))
@@ -80,8 +86,12 @@ class Mixer:
     def dot(self, a, b):
         return self.o.simpson3(np.asarray(a) * np.asarray(b)) / self.o.volume
 
-    def step(self, w, phi):
-        """One iterate(converge) call; returns (new w, err[4], converged)."""
+    def step(self, w, phi, S=None, mop=None):
+        """One iterate(converge) call; returns (new w, err[5], converged).
+        With nmu != 0, S (the oracle's [blk][a*3+b][r] orientation tensor)
+        and mop ([a*3+b][r]) give the Maier-Saupe update
+        M += lambda_m (NMu sum_blk S - M) (SCFT_iterate.f90:351-372); the new
+        tensor is left in self.mop and err[4] = max |NMu S - M|."""
         w = np.asarray(w, dtype=np.float64).reshape(3, -1)
         phi = np.asarray(phi, dtype=np.float64).reshape(3, -1)
         self.n += 1
@@ -89,7 +99,7 @@ class Mixer:
         cp = self.C @ phi
         sw = w.sum(axis=0)
         k = 0 if n <= ns else (n - ns) % (d + 1)
-        err = np.zeros(4)
+        err = np.zeros(5)
         err[3] = np.abs(phi.sum(axis=0) - 1.0).max()
         if n >= ns:  # the last simple iteration fills history slot 0
             wout = cp + (sw - self.fsum) / 3.0
@@ -117,7 +127,12 @@ class Mixer:
                 num = self.dot(dk[K], dk[K])
                 den = self.dot(self.wout[k][K], self.wout[k][K])
                 err[K] = np.sqrt(abs(num / den)) if den != 0 else 0.0
-        strict = bool((err[:3] < self.tol).all())
+        ms = abs(self.nmu) >= 1e-5
+        if ms:
+            d = self.nmu * np.asarray(S).reshape(3, 9, -1).sum(axis=0) - np.asarray(mop).reshape(9, -1)
+            self.mop = np.asarray(mop).reshape(9, -1) + self.lambda_m * d
+            err[4] = np.abs(d).max()
+        strict = bool((err[:3] < self.tol).all()) and (not ms or err[4] < 5 * self.tol)
         relaxed = bool(self.nmu == 0.0 and self.relax_iter > 0 and n >= self.relax_iter
                        and (err[:3] < self.relax_tol).all())
         conv = (strict or relaxed) and n >= self.min_iter

@@ -40,9 +40,10 @@ def test_params_struct_layout():
 
 def test_mix_params_struct_layout():
     # int32 anderson_depth, num_simple; double lambda_simple, lambda_anderson, tol;
-    # int32 min_iter, relax_iter; double relax_tol; int32 reserved[4]
+    # int32 min_iter, relax_iter; double relax_tol, lambda_m; int32 reserved[2]
     assert ctypes.sizeof(wlc.MixParams) == 64
     assert wlc.MixParams.tol.offset == 24 and wlc.MixParams.relax_tol.offset == 40
+    assert wlc.MixParams.lambda_m.offset == 48
 
 
 def _create(**kw):

@@ -101,3 +101,57 @@ def test_cal_scft_converges_and_matches_driver_loop():
     assert out["converged"], (out["n_iter"], errs[-5:])
     assert errs[-1] < 1e-6 and errs[0] > 1e-3
     assert np.isfinite(out["F"])
+
+
+def test_iterate_maier_saupe_tensor():
+    """With NMu != 0 the field update also mixes the Maier-Saupe tensor
+    towards NMu S (simple mixing, lanbtM) and reports its error in err[4];
+    the next sweeps use the updated tensor."""
+    n, L, nmax, ns = 8, 4, 8, (2, 4, 2)
+    nmu, chi = 5.0, (15.0, 15.0, 15.0)
+    dx = 1.0 / n
+    g = wlc.Instance(n, L, nmax, ns, dx, 1.1, (0.5, 0.5, 0.5), chi, nmu=nmu)
+    o = oracle.Oracle((n, n, n), L, nmax, ns, (dx,) * 3, 1.1, (0.5, 0.5, 0.5), chi, nmu=nmu)
+    rng = np.random.default_rng(17)
+    w = rng.normal(0.0, 0.5, size=(3, n ** 3))
+    a = rng.normal(0.0, 0.3, size=(3, 3, n ** 3))
+    m = 0.5 * (a + a.transpose(1, 0, 2))
+    tr = (m[0, 0] + m[1, 1] + m[2, 2]) / 3.0
+    for k in range(3):
+        m[k, k] -= tr
+    g.set_fields(w, m)
+    mp = wlc.mix_params(anderson_depth=2, num_simple=3)
+    mx = Mixer(o, chi, ns, nmax, depth=2, num_simple=3, nmu=nmu)
+    wo, mo = w.copy(), m.reshape(9, -1).copy()
+    for it in range(7):
+        g.MDE_q()
+        g.MDE_qstar()
+        g.density(want_junction=False)
+        err, conv = g.iterate(mp)
+        o.set_fields(wo, mo)
+        o.propagate(1)
+        o.propagate(-1)
+        od = o.density(want_s=True)
+        wo, oerr, oconv = mx.step(wo, od["phi"], od["S"], mo)
+        mo = mx.mop
+        assert rel(g.get_fields(), wo) < 1e-9, it + 1
+        assert rel(g.get_mop().reshape(9, -1), mo) < 1e-9, it + 1
+        assert np.allclose(err, oerr, rtol=1e-8, atol=1e-14), (it + 1, err, oerr)
+        assert conv == oconv
+    assert err[4] > 0.0
+
+
+def test_w_dump_and_readw_round_trip(tmp_path):
+    """W_dump / readW through the reference's file formats restore the
+    fields and the Maier-Saupe tensor exactly."""
+    n = 8
+    g = wlc.Instance(n, 2, 6, (2, 2, 2), 0.12, 1.0, (0.5, 0.5, 0.5), (15.0,) * 3, nmu=3.0)
+    rng = np.random.default_rng(4)
+    w = rng.normal(size=(3, n ** 3))
+    a = rng.normal(size=(3, 3, n ** 3))
+    m = 0.5 * (a + a.transpose(1, 0, 2))
+    g.set_fields(w, m)
+    g.W_dump(tmp_path, rank=0)
+    h = wlc.Instance(n, 2, 6, (2, 2, 2), 0.12, 1.0, (0.5, 0.5, 0.5), (15.0,) * 3, nmu=3.0)
+    h.readW(tmp_path, rank=0)
+    assert np.array_equal(h.get_fields(), w) and np.array_equal(h.get_mop(), m)

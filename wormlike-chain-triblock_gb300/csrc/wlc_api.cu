@@ -588,6 +588,11 @@ struct StepKind {
     int order, sigma, blk;
 };
 
+// Maier-Saupe coupling switched on (|NMu| >= 1e-5, as the reference tests it)
+static bool ms_on(const wlc_ctx* c) { return std::fabs(c->p.nmu) >= 1.0e-5; }
+// orientation tensor accumulated by a streamed backward sweep
+static bool stream_s(const wlc_ctx* c) { return c->p.store_qstar == 2 || ms_on(c); }
+
 static int blk_fwd(const wlc_ctx* c, int s) {  // MDE_ABC.f90:44-57
     if (s <= c->nstart[1]) return 0;
     if (s <= c->nstart[2]) return 1;
@@ -751,7 +756,7 @@ template <typename T> static int sweep(wlc_ctx* c, int dir) {
         }
     } else {
         const DensityArgs d = density_args(c);
-        const int want_s = c->p.store_qstar == 2 ? 1 : 0;
+        const int want_s = stream_s(c) ? 1 : 0;
         if (c->stream) {
             CK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, c->st));
             if (want_s) CK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, c->st));
@@ -835,7 +840,7 @@ extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, 
     if (!c->have_fwd || !c->have_bwd)
         return set_err(c, WLC_E_STATE, "both sweeps (wlc_propagate +1 and -1) must precede wlc_density");
     const size_t nr = (size_t)c->nr;
-    if (s_op && c->p.store_qstar == 0)
+    if (s_op && c->stream && !stream_s(c))
         return set_err(c, WLC_E_STATE, "the orientation tensor is not accumulated with store_qstar = 0 (use 2)");
     const DensityArgs d = density_args(c);
     S3Args s3;
@@ -871,7 +876,7 @@ extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, 
     if (lnq) *lnq = c->lnq;
     if (hflag || !std::isfinite(c->lnq) || !std::isfinite(c->totden))
         return set_err(c, WLC_E_NONFINITE, "non-finite density or partition function");
-    if (s_op) {
+    if (s_op || ms_on(c)) {  // the Maier-Saupe update needs S on the device
         if (!c->stream) {
             if (c->fp32)
                 stensor_launch<float>(c, d);
@@ -882,6 +887,8 @@ extern "C" int wlc_density(wlc_ctx* c, double* phi, double* junc, double* s_op, 
         CK(cudaMemcpyAsync(c->srs, c->sraw, sizeof(double) * 15 * nr, cudaMemcpyDeviceToDevice, c->st));
         launch_scale(c->srs, 15 * (int64_t)nr, c->scal + 1, c->vol, c->st);
         c->launches++;
+    }
+    if (s_op) {
         std::vector<double> h(15 * nr);
         CK(cudaMemcpyAsync(h.data(), c->srs, sizeof(double) * 15 * nr, cudaMemcpyDeviceToHost, c->st));
         CK(cudaStreamSynchronize(c->st));
@@ -1071,6 +1078,14 @@ extern "C" int wlc_get_fields(wlc_ctx* c, double* w) {
     return WLC_OK;
 }
 
+extern "C" int wlc_get_mop(wlc_ctx* c, double* m_op) {
+    if (!ready(c)) return WLC_E_STATE;
+    if (!m_op) return set_err(c, WLC_E_PARAM, "m_op is null");
+    CK(cudaMemcpyAsync(m_op, c->mop, sizeof(double) * 9 * (size_t)c->nr, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return WLC_OK;
+}
+
 extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, int32_t* converged) {
     if (!ready(c)) return WLC_E_STATE;
     if (!mp || !err || !converged) return set_err(c, WLC_E_PARAM, "null argument");
@@ -1078,6 +1093,7 @@ extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, in
     const int depth = mp->anderson_depth;
     if (depth < 1 || depth > kMaxAnderson) return set_err(c, WLC_E_PARAM, "anderson_depth must be in 1..10");
     if (mp->num_simple < 1) return set_err(c, WLC_E_PARAM, "num_simple must be >= 1");
+    if (ms_on(c) && !(mp->lambda_m > 0.0)) return set_err(c, WLC_E_PARAM, "lambda_m must be > 0 when nmu != 0");
     const int64_t nr = c->nr;
     const size_t slot = 3 * (size_t)nr;
     int rc;
@@ -1153,6 +1169,17 @@ extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, in
         for (int K = 0; K < 3; ++K) err[K] = nrm[2 * K + 1] != 0.0 ? std::sqrt(std::fabs(nrm[2 * K] / nrm[2 * K + 1])) : 0.0;
         err[3] = h[3];
     }
+    // Maier-Saupe tensor: simple mixing towards NMu S (SCFT_iterate.f90:351-372;
+    // the reference's Anderson branch for M starts after Num_simple_mixing_M
+    // = 5000 iterations, beyond MAXITS, and never runs)
+    err[4] = 0.0;
+    if (ms_on(c)) {
+        launch_mix_m(c->mop, c->srs, c->p.nmu, mp->lambda_m, nr, maxpart, res + 4, c->st);
+        c->launches += 2;
+        CK(cudaMemcpyAsync(&err[4], res + 4, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        c->have_mop = true;
+    }
     // the fields changed: refresh the BDF3 coefficient planes
     const double third = lit_third(c->real4);
     if (c->fp32)
@@ -1163,7 +1190,8 @@ extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, in
     CK(cudaGetLastError());
     // convergence test (SCFT_iterate.f90:1124-1160) and the minimum iteration
     // count of the driver loop (SCFT_control.f90:270-272)
-    const bool strict = err[0] < mp->tol && err[1] < mp->tol && err[2] < mp->tol;
+    const bool strict = err[0] < mp->tol && err[1] < mp->tol && err[2] < mp->tol &&
+                        (!ms_on(c) || err[4] < 5.0 * mp->tol);
     const bool relaxed = c->p.nmu == 0.0 && mp->relax_iter > 0 && n >= mp->relax_iter && err[0] < mp->relax_tol &&
                          err[1] < mp->relax_tol && err[2] < mp->relax_tol;
     *converged = ((strict || relaxed) && n >= mp->min_iter) ? 1 : 0;
@@ -1393,7 +1421,7 @@ static int batch_build(wlc_batch* b) {
             a.qb = (const float*)c->qb;
             a.sl = (int64_t)c->M * c->nr;
             a.d = density_args(c);
-            a.want_s = c->p.store_qstar == 2 ? 1 : 0;
+            a.want_s = stream_s(c) ? 1 : 0;
             a.jl = c->jl;
             a.raw = c->raw;
             a.junc = c->junc;
@@ -1458,7 +1486,7 @@ static int batch_issue(wlc_batch* b) {
     for (int i : b->streamed) {
         wlc_ctx* c = b->inst[i];
         BCK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, b->st));
-        if (c->p.store_qstar == 2) BCK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, b->st));
+        if (stream_s(c)) BCK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, b->st));
     }
     for (auto* c : b->inst) {
         launch_set_delta<float>(qb_at<float>(c, nmax), c->M, c->nr, b->st);

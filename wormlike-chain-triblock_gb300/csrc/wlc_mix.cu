@@ -88,6 +88,31 @@ __global__ void max_final(const double* __restrict__ part, int nblk, int nq, dou
     }
 }
 
+__global__ void mix_m(double* __restrict__ mop, const double* __restrict__ srs, double nmu, double lambda, int64_t nr,
+                      double* __restrict__ maxpart) {
+    __shared__ double sm[256];
+    double mx = 0.0;
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x) {
+        double t[5] = {0, 0, 0, 0, 0};
+        for (int b = 0; b < 3; ++b)
+            for (int q = 0; q < 5; ++q) t[q] += srs[((int64_t)b * 5 + q) * nr + r];
+        const double S[9] = {t[0], t[2], t[3], t[2], t[1], t[4], t[3], t[4], -(t[0] + t[1])};  // [a + 3b]
+        for (int q = 0; q < 9; ++q) {
+            const double m = mop[(int64_t)q * nr + r];
+            const double d = nmu * S[q] - m;
+            mop[(int64_t)q * nr + r] = m + lambda * d;
+            mx = fmax(mx, fabs(d));
+        }
+    }
+    sm[threadIdx.x] = mx;
+    __syncthreads();
+    for (int s = 128; s > 0; s >>= 1) {
+        if (threadIdx.x < s) sm[threadIdx.x] = fmax(sm[threadIdx.x], sm[threadIdx.x + s]);
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) maxpart[blockIdx.x] = sm[0];
+}
+
 constexpr int kDotThreads = 128;
 
 // Anderson inner products in one pass over the history (SCFT_iterate.f90:237-276):
@@ -244,6 +269,12 @@ void launch_mix_out(const double* phi, double* w, const MixChi& chi, int64_t nr,
                     double* dw, double* maxpart, double* maxout, cudaStream_t st) {
     mix_out<<<kMixBlocks, 256, 0, st>>>(phi, w, chi, nr, mode, lambda, wout, dw, maxpart);
     max_final<<<1, 256, 0, st>>>(maxpart, kMixBlocks, 4, maxout);
+}
+
+void launch_mix_m(double* mop, const double* srs, double nmu, double lambda, int64_t nr, double* maxpart,
+                  double* maxout, cudaStream_t st) {
+    mix_m<<<kMixBlocks, 256, 0, st>>>(mop, srs, nmu, lambda, nr, maxpart);
+    max_final<<<1, 256, 0, st>>>(maxpart, kMixBlocks, 1, maxout);
 }
 
 int anderson_acc_count(int nrt) { return nrt * (nrt + 1) / 2 + nrt + 6; }

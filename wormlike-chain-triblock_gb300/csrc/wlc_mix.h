@@ -35,6 +35,12 @@ struct AndersonSlots {
 
 void launch_mix_out(const double* phi, double* w, const MixChi& chi, int64_t nr, int mode, double lambda, double* wout,
                     double* dw, double* maxpart, double* maxout, cudaStream_t st);
+// Maier-Saupe tensor update by simple mixing (SCFT_iterate.f90:351-372):
+// M_ab += lambda (NMu S_ab - M_ab) for the 9 components, S the orientation
+// tensor summed over the blocks (srs[blk][t][r], t = xx, yy, xy, xz, yz;
+// S_zz = -S_xx - S_yy); max |NMu S - M| into *maxout
+void launch_mix_m(double* mop, const double* srs, double nmu, double lambda, int64_t nr, double* maxpart,
+                  double* maxout, cudaStream_t st);
 // U_mn = <dW_k - dW_km, dW_k - dW_kn>, V_m = <dW_k - dW_km, dW_k> (summed over the
 // blocks), then <dW_k,K, dW_k,K> and <w_out_k,K, w_out_k,K> per block K: out[0 .. nacc)
 int anderson_acc_count(int nrt);

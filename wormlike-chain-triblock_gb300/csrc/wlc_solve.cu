@@ -163,6 +163,16 @@ __device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, 
     }
 }
 
+// asynchronous global -> shared copy of one complex element (cp.async:
+// the column loads are all in flight before the tables are staged)
+template <typename C> __device__ __forceinline__ void cp_async_elem(C* sdst, const C* gsrc) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
+    if constexpr (sizeof(C) == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sa), "l"(gsrc) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(sa), "l"(gsrc) : "memory");
+}
+
 template <typename X> __device__ __forceinline__ void stage(X* dst, const X* src, int n) {
     for (int e = threadIdx.x; e < n; e += blockDim.x) dst[e] = src[e];
 }
@@ -189,6 +199,10 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
     int8_t* s_dra = reinterpret_cast<int8_t*>(smem_raw + sm.dr_axis);
     float* s_drv = reinterpret_cast<float*>(smem_raw + sm.dr_valf);
     float2* corr = reinterpret_cast<float2*>(smem_raw + sm.corr);
+    const int colid = blockIdx.x;
+    C* gcol = a.phat + (size_t)colid * M * N;
+    for (int e = threadIdx.x; e < M * N; e += blockDim.x) cp_async_elem(col + (e / N) * NP + (e % N), gcol + e);
+    asm volatile("cp.async.commit_group;\n" ::: "memory");
     stage(s_zoff, g.zoff, M);
     if (correct) {
         stage(s_zofff, g.zofff, M);
@@ -197,13 +211,10 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
         stage(s_dra, g.dr_axis, g.ndr);
         stage(s_drv, g.dr_valf, g.ndr);
     }
-    const int colid = blockIdx.x;
     const int kyi = colid / a.nkx, kxi = colid % a.nkx;
     const int ix = fold_n(kxi, N), iy = fold_n(kyi, N);
     const double kx = ix * a.kf[0], ky = iy * a.kf[1];
     const double rho = sqrt(kx * kx + ky * ky);
-    C* gcol = a.phat + (size_t)colid * M * N;
-    for (int e = threadIdx.x; e < M * N; e += blockDim.x) col[(e / N) * NP + (e % N)] = gcol[e];
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
     if (threadIdx.x == 0) {
         const double ca = rho > 0 ? kx / rho : 1.0, sa = rho > 0 ? ky / rho : 0.0;
@@ -218,6 +229,7 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
             sm2 = sn;
         }
     }
+    asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     __syncthreads();
     fft_nat2perm<N, -1>(col, M, 1, NP, tw);
 

@@ -28,17 +28,18 @@ _LIB = None
 WLC_FP64, WLC_FP32 = 0, 1
 WLC_LIT_REAL4, WLC_LIT_REAL8 = 0, 1
 ERRORS = {-1: "WLC_E_PARAM", -2: "WLC_E_ALLOC", -3: "WLC_E_CUDA", -4: "WLC_E_STATE",
-          -5: "WLC_E_NONFINITE", -6: "WLC_E_UNSUPPORTED", -7: "WLC_E_SELFTEST"}
+          -5: "WLC_E_NONFINITE", -6: "WLC_E_UNSUPPORTED", -7: "WLC_E_SELFTEST", -8: "WLC_E_IO"}
 
 # exported symbols declared in include/wlc.h
 SYMBOLS = ["wlc_abi_version", "wlc_create", "wlc_destroy", "wlc_last_error", "wlc_set_box",
            "wlc_set_fields", "wlc_propagate", "wlc_density", "wlc_free_energy", "wlc_get_q",
            "wlc_set_q", "wlc_init_pr", "wlc_mde_one_step", "wlc_launch_count", "wlc_stream",
            "wlc_enable_timing", "wlc_last_timing", "wlc_iterate", "wlc_reset_mixing", "wlc_get_fields",
-           "wlc_set_precision", "wlc_autotune", "wlc_set_launch_config", "wlc_batch_create",
+           "wlc_set_precision", "wlc_get_mop", "wlc_autotune", "wlc_set_launch_config", "wlc_batch_create",
            "wlc_batch_destroy", "wlc_batch_last_error", "wlc_batch_size", "wlc_batch_groups", "wlc_batch_get",
            "wlc_batch_propagate", "wlc_batch_autotune", "wlc_batch_use_graph", "wlc_batch_stream",
-           "wlc_batch_launch_count"]
+           "wlc_batch_launch_count", "wlc_io_write_w", "wlc_io_read_w", "wlc_io_write_mop", "wlc_io_read_mop",
+           "wlc_io_write_rho", "wlc_io_append_free_energy", "wlc_io_append_errors"]
 
 
 class WlcError(RuntimeError):
@@ -61,15 +62,16 @@ class MixParams(ctypes.Structure):
     _fields_ = [("anderson_depth", ctypes.c_int32), ("num_simple", ctypes.c_int32),
                 ("lambda_simple", ctypes.c_double), ("lambda_anderson", ctypes.c_double),
                 ("tol", ctypes.c_double), ("min_iter", ctypes.c_int32), ("relax_iter", ctypes.c_int32),
-                ("relax_tol", ctypes.c_double), ("reserved", ctypes.c_int32 * 4)]
+                ("relax_tol", ctypes.c_double), ("lambda_m", ctypes.c_double), ("reserved", ctypes.c_int32 * 2)]
 
 
 def mix_params(anderson_depth=5, num_simple=20, lambda_simple=0.1, lambda_anderson=0.1, tol=1e-4,
-               min_iter=20, relax_iter=150, relax_tol=5e-4):
+               min_iter=20, relax_iter=150, relax_tol=5e-4, lambda_m=0.08):
     m = MixParams()
     m.anderson_depth, m.num_simple = int(anderson_depth), int(num_simple)
     m.lambda_simple, m.lambda_anderson, m.tol = float(lambda_simple), float(lambda_anderson), float(tol)
     m.min_iter, m.relax_iter, m.relax_tol = int(min_iter), int(relax_iter), float(relax_tol)
+    m.lambda_m = float(lambda_m)
     return m
 
 
@@ -116,6 +118,16 @@ def load(build_if_missing=True):
     lib.wlc_reset_mixing.argtypes = [P]
     lib.wlc_get_fields.argtypes = [P, Dp]
     lib.wlc_set_precision.argtypes = [P, I]
+    lib.wlc_get_mop.argtypes = [P, Dp]
+    C = ctypes.c_char_p
+    L64 = ctypes.c_int64
+    lib.wlc_io_write_w.argtypes = [C, Dp, L64]
+    lib.wlc_io_read_w.argtypes = [C, Dp, L64]
+    lib.wlc_io_write_mop.argtypes = [C, Dp, L64, Dp]
+    lib.wlc_io_read_mop.argtypes = [C, Dp, L64]
+    lib.wlc_io_write_rho.argtypes = [C, Dp, ctypes.POINTER(ctypes.c_int32), Dp]
+    lib.wlc_io_append_free_energy.argtypes = [C, I, D, D, D, Dp, ctypes.POINTER(ctypes.c_int32), I]
+    lib.wlc_io_append_errors.argtypes = [C, I, Dp, I]
     Ip = ctypes.POINTER(ctypes.c_int32)
     lib.wlc_autotune.argtypes = [P, Ip]
     lib.wlc_set_launch_config.argtypes = [P, I, I]
@@ -332,10 +344,10 @@ class Instance:
     # ---------------------------------------------------------- SCFT loop
     def iterate(self, mix=None, **kw):
         """iterate(converge) (SCFT_iterate.f90:27-334, three-block form) on the
-        device; returns (err[4], converged).  err[0..2] block errors, err[3]
-        max |sum_K phi_K - 1|."""
+        device; returns (err[5], converged).  err[0..2] block errors, err[3]
+        max |sum_K phi_K - 1|, err[4] the Maier-Saupe tensor error (nmu != 0)."""
         mp = mix if mix is not None else mix_params(**kw)
-        err = np.zeros(4)
+        err = np.zeros(5)
         conv = ctypes.c_int32(0)
         self._check(self.lib.wlc_iterate(self.h, ctypes.byref(mp), _dp(err), ctypes.byref(conv)))
         return err, bool(conv.value)
@@ -357,6 +369,25 @@ class Instance:
 
     def reset_mixing(self):
         self._check(self.lib.wlc_reset_mixing(self.h))
+
+    def W_dump(self, directory=".", rank=0):
+        """W_dump (SCFT_dump.f90:273-308): W<rank>.dat and M_OP<rank>.dat."""
+        box = [self.params.dx[a] * self.n[a] for a in range(3)]
+        io.write_w(os.path.join(directory, "W%d.dat" % rank), self.get_fields())
+        io.write_mop(os.path.join(directory, "M_OP%d.dat" % rank), self.get_mop(), box)
+
+    def readW(self, directory=".", rank=0):
+        """readW (init_array_2dcomp_mod.f90:1070-1106): fields and M_OP from
+        W<rank>.dat / M_OP<rank>.dat (M_OP optional)."""
+        w = io.read_w(os.path.join(directory, "W%d.dat" % rank), self.nr)
+        mpath = os.path.join(directory, "M_OP%d.dat" % rank)
+        self.set_fields(w, io.read_mop(mpath, self.nr) if os.path.exists(mpath) else None)
+
+    def get_mop(self):
+        """M_OP as a (3, 3, nr) array [b][a][r] (symmetric)."""
+        m = np.empty((3, 3, self.nr))
+        self._check(self.lib.wlc_get_mop(self.h, _dp(m)))
+        return m
 
     def get_fields(self):
         w = np.empty((3, self.nr))
@@ -454,3 +485,55 @@ class Batch:
             self.close()
         except Exception:
             pass
+
+
+class io:
+    """The reference's files (W<rank>.dat, M_OP<rank>.dat, RHO_total.dat,
+    FreeEG.dat, error.dat) through libwlc's host-side readers and writers."""
+
+    @staticmethod
+    def _rc(rc, what):
+        if rc != 0:
+            raise WlcError(rc, what)
+
+    @staticmethod
+    def write_w(path, w):
+        w = np.ascontiguousarray(w, dtype=np.float64).reshape(3, -1)
+        io._rc(load().wlc_io_write_w(os.fsencode(path), _dp(w), w.shape[1]), "write " + str(path))
+
+    @staticmethod
+    def read_w(path, nr):
+        w = np.empty((3, nr))
+        io._rc(load().wlc_io_read_w(os.fsencode(path), _dp(w), nr), "read " + str(path))
+        return w
+
+    @staticmethod
+    def write_mop(path, m_op, box):
+        m = np.ascontiguousarray(m_op, dtype=np.float64).reshape(9, -1)
+        b = np.ascontiguousarray(box, dtype=np.float64).reshape(3)
+        io._rc(load().wlc_io_write_mop(os.fsencode(path), _dp(m), m.shape[1], _dp(b)), "write " + str(path))
+
+    @staticmethod
+    def read_mop(path, nr):
+        m = np.empty((3, 3, nr))
+        io._rc(load().wlc_io_read_mop(os.fsencode(path), _dp(m), nr), "read " + str(path))
+        return m
+
+    @staticmethod
+    def write_rho(path, phi, n, dx):
+        phi = np.ascontiguousarray(phi, dtype=np.float64).reshape(3, -1)
+        nn = (ctypes.c_int32 * 3)(*[int(v) for v in n])
+        d = np.ascontiguousarray(dx, dtype=np.float64).reshape(3)
+        io._rc(load().wlc_io_write_rho(os.fsencode(path), _dp(phi), nn, _dp(d)), "write " + str(path))
+
+    @staticmethod
+    def append_free_energy(path, n_iter, fe, lnq, box, chi, ns, nmax):
+        c = np.ascontiguousarray(chi, dtype=np.float64).reshape(3)
+        nn = (ctypes.c_int32 * 3)(*[int(v) for v in ns])
+        io._rc(load().wlc_io_append_free_energy(os.fsencode(path), int(n_iter), float(fe), float(lnq), float(box),
+                                                _dp(c), nn, int(nmax)), "append " + str(path))
+
+    @staticmethod
+    def append_errors(path, n_iter, err):
+        e = np.ascontiguousarray(err, dtype=np.float64).reshape(-1)
+        io._rc(load().wlc_io_append_errors(os.fsencode(path), int(n_iter), _dp(e), len(e)), "append " + str(path))
