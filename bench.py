@@ -387,6 +387,15 @@ def run_converge(args):
     nr = wl["n"] ** 3
     rng = np.random.default_rng(2024)
     w0 = rng.normal(0.0, wl["w_sigma"], size=(3, nr))
+    if args.seed_kind == "lamellar":
+        # lamellar start: A and C stripes in antiphase along x, B between them,
+        # amplitude 1.0, plus seeded N(0, 0.1^2) noise
+        n = wl["n"]
+        x = (np.arange(nr) % n) / n
+        c1, c2 = np.cos(2 * np.pi * x), np.cos(4 * np.pi * x)
+        w0 = np.stack([c1, c2, -c1]) + rng.normal(0.0, 0.1, size=(3, nr))
+    if args.init_w:  # restart from saved fields (the reference's readW restart)
+        w0 = np.load(args.init_w)
     mp = wlc.mix_params(anderson_depth=args.depth, num_simple=20, lambda_anderson=args.lambda_a, tol=args.tol,
                         min_iter=20, relax_iter=0)
     out = {"metric": "time-to-converged F (64^3, L=10, Ns=200, ABC; residual <= %g)" % args.tol,
@@ -403,6 +412,8 @@ def run_converge(args):
         hist, switched, n, conv = [], None, 0, False
         t_switch = None
         while not conv and n < args.max_iter and time.perf_counter() - t0 < args.budget:
+            if args.stop_at > 0 and hist and max(hist[-1][3:6]) < args.stop_at and n > 20:
+                break
             n += 1
             if args.ramp and n > 20:  # lambda_A = max(lambda_a, 1 - 0.9^(n - 20))
                 mp.lambda_anderson = max(args.lambda_a, 1.0 - 0.9 ** (n - 20))
@@ -418,7 +429,26 @@ def run_converge(args):
                 t_switch = time.perf_counter() - t0
         torch.cuda.synchronize()
         secs = time.perf_counter() - t0
+        if args.save_w:
+            np.save(args.save_w, inst.get_fields())
+        fp32_err = None
+        if prec == wlc.WLC_FP32 and switched is None:
+            # the FP32 form's error at its final fields: the same fields
+            # evaluated by the FP64 propagators
+            w_fin = inst.get_fields()
+            vals = {}
+            for pr in (wlc.WLC_FP32, wlc.WLC_FP64):
+                inst.set_precision(pr)
+                inst.set_fields(w_fin)
+                inst.MDE_q()
+                inst.MDE_qstar()
+                dd = inst.density(want_junction=False)
+                vals[pr] = (dd["lnQ"], inst.free_energy(), dd["phi"])
+            a32, a64 = vals[wlc.WLC_FP32], vals[wlc.WLC_FP64]
+            fp32_err = {"lnQ_abs": abs(a32[0] - a64[0]), "F_rel": abs(a32[1] - a64[1]) / abs(a64[1]),
+                        "phi_max_rel": float(np.abs(a32[2] - a64[2]).max() / np.abs(a64[2]).max())}
         out["forms"][form] = {"converged": bool(conv), "iterations": n, "seconds": secs, "F": hist[-1][1],
+                              "fp32_error_vs_fp64": fp32_err,
                               "lnQ": hist[-1][2], "residual": max(hist[-1][3:6]), "incompressibility": hist[-1][6],
                               "switched_at": switched, "switch_seconds": t_switch,
                               "s_per_iteration": secs / max(1, n)}
@@ -554,6 +584,10 @@ def main():
     ap.add_argument("--budget", type=float, default=900.0, help="wall-time cap per form, seconds")
     ap.add_argument("--history", action="store_true")
     ap.add_argument("--lambda-a", type=float, default=0.1, help="Anderson mixing parameter")
+    ap.add_argument("--init-w", default="", help="start from fields saved with --save-w (.npy)")
+    ap.add_argument("--seed-kind", default="random", choices=["random", "lamellar"])
+    ap.add_argument("--save-w", default="", help="save the final fields (.npy)")
+    ap.add_argument("--stop-at", type=float, default=0.0, help="stop once the residual is below this")
     ap.add_argument("--ramp", action="store_true", help="ramp lambda_A towards 1 after the simple phase")
     args = ap.parse_args()
     if args.profile:
