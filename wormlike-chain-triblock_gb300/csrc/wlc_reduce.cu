@@ -109,6 +109,22 @@ __global__ void ms_term(const T* __restrict__ h1, const T* __restrict__ h2, cons
 // ------------------------------------------------------------ densities
 // raw[b][r] = sum_i S1_{s in block b}(q_i q*_i); junc[j][r] = sum_i q_i q*_i at
 // s = NA, NA+NB, Nmax; qend[r] = q_0(r, Nmax).
+// sum_i a[i*stride] c[i*stride] in FP64 with four independent partial sums
+// (more loads in flight per thread; fixed order, so deterministic)
+template <typename T>
+__device__ __forceinline__ double dot_coeffs(const T* __restrict__ a, const T* __restrict__ c, int M, int64_t stride) {
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int i = 0;
+    for (; i + 4 <= M; i += 4) {
+        s0 += (double)a[i * stride] * (double)c[i * stride];
+        s1 += (double)a[(i + 1) * stride] * (double)c[(i + 1) * stride];
+        s2 += (double)a[(i + 2) * stride] * (double)c[(i + 2) * stride];
+        s3 += (double)a[(i + 3) * stride] * (double)c[(i + 3) * stride];
+    }
+    for (; i < M; ++i) s0 += (double)a[i * stride] * (double)c[i * stride];
+    return (s0 + s1) + (s2 + s3);
+}
+
 template <typename T>
 __global__ void density_accum(const T* __restrict__ qf, const T* __restrict__ qb, DensityArgs d,
                               double* __restrict__ raw, double* __restrict__ junc, double* __restrict__ qend) {
@@ -122,10 +138,7 @@ __global__ void density_accum(const T* __restrict__ qf, const T* __restrict__ qb
                 for (int s = s0; s <= s0 + n; ++s) {
                     const int j = s - s0;
                     const double wgt = (j == 0 || j == n) ? 1.0 : ((j & 1) ? 4.0 : 2.0);
-                    double sum = 0.0;
-                    const T* a = qf + s * sl + r;
-                    const T* c = qb + s * sl + r;
-                    for (int i = 0; i < d.M; ++i) sum += (double)a[i * nr] * (double)c[i * nr];
+                    const double sum = dot_coeffs(qf + s * sl + r, qb + s * sl + r, d.M, nr);
                     acc += wgt * sum;
                 }
                 acc *= d.ds / 3.0;
@@ -134,11 +147,7 @@ __global__ void density_accum(const T* __restrict__ qf, const T* __restrict__ qb
         }
         const int sj[3] = {d.nstart[1], d.nstart[2], d.nmax};
         for (int j = 0; j < 3; ++j) {
-            double sum = 0.0;
-            const T* a = qf + sj[j] * sl + r;
-            const T* c = qb + sj[j] * sl + r;
-            for (int i = 0; i < d.M; ++i) sum += (double)a[i * nr] * (double)c[i * nr];
-            junc[j * nr + r] = sum;
+            junc[j * nr + r] = dot_coeffs(qf + sj[j] * sl + r, qb + sj[j] * sl + r, d.M, nr);
         }
         qend[r] = (double)qf[(int64_t)d.nmax * sl + r];
     }
@@ -195,8 +204,7 @@ __device__ __forceinline__ void density_slice_body(const T* __restrict__ a, cons
     const bool last = s == 0;
     const double sc = d.ds / 3.0;
     for (int64_t r = r0; r < nr; r += rstep) {
-        double sum = 0.0;
-        for (int i = 0; i < d.M; ++i) sum += (double)a[i * nr + r] * (double)c[i * nr + r];
+        const double sum = dot_coeffs(a + r, c + r, d.M, nr);
         if (any)
             for (int b = 0; b < 3; ++b)
                 if (wgt[b] != 0.0) raw[b * nr + r] += wgt[b] * sum;
