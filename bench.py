@@ -355,6 +355,22 @@ def run_profile_case(args):
     density pass; a few GB of device memory."""
     import wlc
     wl = workload(args.precision)
+    if args.workload == "large":  # the large workload's grid and L on a 6-step chain, K = 3
+        n = 128
+        inst = wlc.Instance(n, 12, 6, (2, 2, 2), 8.0 * wlc.wlc_radius_of_gyration(4.0) / n, 2.0, (0.5, 0.5, 0.5),
+                            (20.0, 20.0, 20.0), nmu=5.0, precision=wlc.WLC_FP32, store_qstar=2, q_checkpoint=3)
+        rng = np.random.default_rng(5)
+        inst.set_fields(rng.normal(0.0, 0.5, size=(3, n ** 3)), rng.normal(0.0, 0.1, size=(3, 3, n ** 3)))
+        if args.launch_config:
+            inst.set_launch_config(*(int(v) for v in args.launch_config.split(",")))
+        inst.MDE_q()
+        inst.MDE_qstar()
+        d = inst.density(want_junction=False)
+        inst.free_energy()
+        inst.iterate(wlc.mix_params())
+        print(json.dumps({"profile_case": "large", "lnQ": d["lnQ"], "launches": inst.launch_count}))
+        inst.close()
+        return
     inst = wlc.Instance(wl["n"], wl["L"], 6, (2, 2, 2), wl["dx"], wl["loa"], wl["kappa"], wl["chi"],
                         precision=wlc.WLC_FP64 if args.precision == "fp64" else wlc.WLC_FP32)
     rng = np.random.default_rng(5)
@@ -562,6 +578,75 @@ def run_batch(args):
     b.close()
 
 
+def run_large(args):
+    """Large single instance with contour checkpointing: 128^3, box 8.0 Rg,
+    l <= 12 (169 coefficients), Ns = 400 (120/160/120), chiN = 20,
+    contour/persistence = 4.0, Maier-Saupe muN = 5, gyroid-like start (sum
+    of sin.cos terms, amplitude 1.0, plus N(0, 0.05^2)); FP32 propagators,
+    FP64 reductions; q kept at every K-th slice (K ~ sqrt(3 Ns)) and
+    recomputed per segment in the backward sweep, densities and the
+    orientation tensor streamed.  One bench step = forward sweep + backward
+    sweep with segment recompute + densities + free energy + field update
+    (3 Ns contour steps, 2 Ns of them the MDE sweeps proper)."""
+    import torch
+    import wlc
+    x = 4.0
+    n, L, nmax = 128, 12, 400
+    box = 8.0 * wlc.wlc_radius_of_gyration(x)
+    ns = wlc.even_block_lengths((0.3, 0.4, 0.3), nmax)
+    K = args.checkpoint or int(round((3 * nmax) ** 0.5))
+    inst = wlc.Instance(n, L, nmax, ns, box / n, x * 0.5, (0.5, 0.5, 0.5), (20.0, 20.0, 20.0), nmu=5.0,
+                        precision=wlc.WLC_FP32, store_qstar=2, q_checkpoint=K)
+    g = 2 * np.pi * np.arange(n) / n
+    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+    gyr = (np.sin(X) * np.cos(Y) + np.sin(Y) * np.cos(Z) + np.sin(Z) * np.cos(X)).transpose(2, 1, 0).reshape(-1)
+    rng = np.random.default_rng(77)
+    w = np.stack([gyr, -gyr, 0.5 * gyr]) + rng.normal(0.0, 0.05, size=(3, n ** 3))
+    inst.set_fields(w)
+    tuned = None if args.no_autotune else inst.autotune()
+    stream = torch.cuda.ExternalStream(inst.stream)
+    mp = wlc.mix_params(anderson_depth=5)
+
+    def step():
+        inst.MDE_q()
+        inst.MDE_qstar()
+        inst.density(want_junction=False)
+        fe = inst.free_energy()
+        err, _ = inst.iterate(mp)
+        return fe, err
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    clk = ClockSampler(0)
+    clk.start()
+    l0 = inst.launch_count
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        fe, err = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = e0.elapsed_time(e1)
+    mde_steps = 2 * nmax * args.steps
+    free, total = torch.cuda.mem_get_info()
+    line = {"metric": "MDE contour steps/s (128^3, L=12, Ns=400, sqrt(Ns) checkpointing, Maier-Saupe)",
+            "value": mde_steps / (ms / 1000.0), "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (gyroid-like seeded start)",
+            "config": {"workload": "ABC triblock 128^3, box 8.0 Rg, L=12 (M=169), Ns=400 (%d/%d/%d), chiN=20, "
+                                   "L/lp=4.0, muN=5; q checkpoint every %d slices, recompute per segment; one bench "
+                                   "step = one SCFT iteration (%d MDE steps + %d recompute steps)" % (
+                                       ns[0], ns[1], ns[2], K, 2 * nmax, nmax - nmax // K),
+                       "l2": "inputs larger than L2 (1.4 GB per slice)",
+                       "launch_config": tuned},
+            "device_memory_used_gb": (total - free) / 1e9, "F": fe, "residual": float(max(err[:3])),
+            "gpu_launches": int(inst.launch_count - l0), "clocks": clocks}
+    print(json.dumps(line))
+    inst.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -572,7 +657,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="small-footprint case for ncu captures")
     ap.add_argument("--converge", action="store_true", help="time-to-converged F instead of steps/s")
-    ap.add_argument("--workload", default="single", choices=["single", "batch"])
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "large"])
+    ap.add_argument("--checkpoint", type=int, default=0, help="large workload: q checkpoint interval")
     ap.add_argument("--count", type=int, default=48, help="instances of the batched workload")
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration")
     ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads")
@@ -598,6 +684,9 @@ def main():
         return
     if args.workload == "batch" and args.impl == "ours":
         run_batch(args)
+        return
+    if args.workload == "large" and args.impl == "ours":
+        run_large(args)
         return
     wl = workload(args.precision)
     if args.impl == "reference":

@@ -434,6 +434,7 @@ static int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
     *out = c;
     if (!build_basis_tables(c->L, c->real4, c->tab, why)) return set_err(c, WLC_E_SELFTEST, why);
     if ((rc = check_smem(c, c->fp32))) return rc;
+    prepare_reduce_kernels();
     if (ext) {
         c->st = ext;
         c->own_stream = false;
@@ -464,6 +465,12 @@ static int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
         if ((rc = upload(c, &pd, tv))) return rc;
         c->thl.val = pd;
         c->thl.n = (int)tr.size();
+        std::vector<int> rp(M + 1, 0);  // entries are emitted row by row
+        for (int16_t i : tr) rp[i + 1]++;
+        for (int i = 0; i < M; ++i) rp[i + 1] += rp[i];
+        int* pr;
+        if ((rc = upload(c, &pr, rp))) return rc;
+        c->thl.rowptr = pr;
         std::vector<int> jp(6, 0);
         std::vector<int16_t> jr, jc;
         std::vector<double> jv;
@@ -484,6 +491,7 @@ static int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
         c->jl.col = p16;
         if ((rc = upload(c, &pd, jv))) return rc;
         c->jl.val = pd;
+        c->jl.n = (int)jv.size();
     }
     c->nkeys = 3 * (c->N / 2) * (c->N / 2) + 1;
     c->npiv = (c->L + 1) * (c->L + 2) / 2;
@@ -1473,7 +1481,10 @@ static int batch_issue(wlc_batch* b) {
     };
     auto slices = [&](int s) {
         if (b->streamed.empty()) return;
-        launch_density_slice_batched<float>(b->dslice, (int)b->streamed.size(), b->max_nr_streamed, s, b->st);
+        bool any_s = false;
+        for (int i : b->streamed) any_s = any_s || stream_s(b->inst[i]);
+        launch_density_slice_batched<float>(b->dslice, (int)b->streamed.size(), b->max_nr_streamed, s, b->M,
+                                            b->inst[b->streamed[0]]->jl.n, any_s ? 1 : 0, b->st);
         b->launches++;
     };
     int rc;

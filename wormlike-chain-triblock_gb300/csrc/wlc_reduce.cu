@@ -77,31 +77,65 @@ __global__ void make_cf(const double* __restrict__ w, T* __restrict__ cf, double
 // Maier-Saupe term ds * sum_j Theta_ij(r) h_j(r), h the BDF history
 // combination of the given order (calc_THETAij and the Theta loop of
 // init_pr, wormlike_MDE_2dcomp_mod.f90:5-110, MDE_ABC.f90:256-268).
+// shared-memory layout of ms_term: val[5n] | hc[M][TILE] | rowptr[M+1] | col[n]
+template <typename T> __host__ __device__ inline size_t ms_smem_bytes(int n, int M) {
+    return sizeof(T) * ((size_t)5 * n + (size_t)M * PointTile<T>::value) + sizeof(int) * (size_t)(M + 1) +
+           sizeof(int16_t) * (size_t)n;
+}
+
+// The Theta lists (values converted to the compute type) are staged once per
+// CTA; the CTA then walks tiles of TILE points.  Thread (k, g) handles point
+// k of the tile and rows i = g, g + kMsGroups, ... of its output.
 template <typename T>
-__global__ void ms_term(const T* __restrict__ h1, const T* __restrict__ h2, const T* __restrict__ h3, int order,
-                        const double* __restrict__ mop, ThetaLists tl, double ds, double thresh, int M, int64_t nr,
-                        T* __restrict__ out) {
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x) {
-        const double a0 = mop[0 * nr + r] - mop[4 * nr + r];  // M00 - M11
-        const double coef[5] = {a0, mop[8 * nr + r], mop[3 * nr + r], mop[6 * nr + r], mop[7 * nr + r]};
-        // note M01 = mop[(0 + 3*1)] = M_OP(k,0,1) in Fortran order; the tensor is symmetric
-        for (int i = 0; i < M; ++i) out[(int64_t)i * nr + r] = (T)0;
-        // Theta_ij(r) = sum_c coef_c T_c(i,j), thresholded per entry
-        for (int e = 0; e < tl.n; ++e) {
-            const int i = tl.row[e], j = tl.col[e];
-            double th = 0.0;
-            for (int c = 0; c < 5; ++c) th += coef[c] * tl.val[5 * e + c];
-            if (fabs(th) < thresh) continue;
-            double hj;
-            const int64_t o = (int64_t)j * nr + r;
-            if (order == 1)
-                hj = (double)h1[o];
-            else if (order == 2)
-                hj = 2.0 * (double)h1[o] - (double)h2[o];
-            else
-                hj = 3.0 * (double)h1[o] - 3.0 * (double)h2[o] + (double)h3[o];
-            const int64_t oi = (int64_t)i * nr + r;
-            out[oi] = (T)((double)out[oi] + ds * th * hj);
+__global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
+    ms_term(const T* __restrict__ h1, const T* __restrict__ h2, const T* __restrict__ h3, int order,
+            const double* __restrict__ mop, ThetaLists tl, double ds, double thresh, int M, int64_t nr,
+            T* __restrict__ out) {
+    constexpr int TILE = PointTile<T>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    T* sval = reinterpret_cast<T*>(smem_raw);
+    T* hc = sval + (size_t)5 * tl.n;  // [M][TILE]: BDF history combination of the tile's points
+    int* srp = reinterpret_cast<int*>(hc + (size_t)M * TILE);
+    int16_t* scol = reinterpret_cast<int16_t*>(srp + M + 1);
+    for (int e = threadIdx.x; e < 5 * tl.n; e += blockDim.x) sval[e] = (T)tl.val[e];
+    for (int e = threadIdx.x; e <= M; e += blockDim.x) srp[e] = tl.rowptr[e];
+    for (int e = threadIdx.x; e < tl.n; e += blockDim.x) scol[e] = tl.col[e];
+    const int k = threadIdx.x % TILE, g = threadIdx.x / TILE;
+    const T th_min = (T)thresh;
+    for (int64_t r0 = (int64_t)blockIdx.x * TILE; r0 < nr; r0 += (int64_t)gridDim.x * TILE) {
+        __syncthreads();  // tables staged / previous tile consumed
+        for (int idx = threadIdx.x; idx < M * TILE; idx += blockDim.x) {
+            const int j = idx / TILE, kk = idx % TILE;
+            const int64_t r = r0 + kk;
+            T v = (T)0;
+            if (r < nr) {
+                const int64_t o = (int64_t)j * nr + r;
+                if (order == 1)
+                    v = h1[o];
+                else if (order == 2)
+                    v = (T)2 * h1[o] - h2[o];
+                else
+                    v = (T)3 * h1[o] - (T)3 * h2[o] + h3[o];
+            }
+            hc[idx] = v;
+        }
+        __syncthreads();
+        const int64_t r = r0 + k;
+        if (r >= nr) continue;
+        // Theta_ij(r) = sum_c coef_c T_c(i,j), entries below the threshold dropped
+        // (M01 = mop[0 + 3*1] = M_OP(k,0,1) in Fortran order; the tensor is symmetric)
+        const T coef[5] = {(T)(mop[0 * nr + r] - mop[4 * nr + r]), (T)mop[8 * nr + r], (T)mop[3 * nr + r],
+                           (T)mop[6 * nr + r], (T)mop[7 * nr + r]};
+        const T* hv = hc + k;
+        for (int i = g; i < M; i += kMsGroups) {
+            T acc = (T)0;
+            for (int e = srp[i]; e < srp[i + 1]; ++e) {
+                const T* v5 = sval + 5 * e;
+                const T th = coef[0] * v5[0] + coef[1] * v5[1] + coef[2] * v5[2] + coef[3] * v5[3] + coef[4] * v5[4];
+                if (fabs(th) < th_min) continue;
+                acc += th * hv[scol[e] * TILE];
+            }
+            out[(int64_t)i * nr + r] = (T)ds * acc;
         }
     }
 }
@@ -153,42 +187,115 @@ __global__ void density_accum(const T* __restrict__ qf, const T* __restrict__ qb
     }
 }
 
-// orientation tensor per block (SCFT_Density_FE.f90:161-220):
-// sraw[b][t][r] = S1_s( q^T J_t q* ), t = 11, 22, 12, 13, 23
+// shared-memory layout of the tiled density / tensor kernels:
+// sa[M][TILE] | sc[M][TILE] | jval[nj] | jptr[6] | jrow[nj] | jcol[nj]
+template <typename T> __host__ __device__ inline size_t slice_smem_bytes(int M, int nj, bool want_s) {
+    size_t b = 2 * sizeof(T) * (size_t)M * PointTile<T>::value;
+    if (want_s) b += sizeof(T) * (size_t)nj + sizeof(int) * 6 + 2 * sizeof(int16_t) * (size_t)nj;
+    return b;
+}
+
+template <typename T> struct SliceSmem {
+    T* sa;
+    T* sc;
+    T* jval;
+    int* jptr;
+    int16_t* jrow;
+    int16_t* jcol;
+};
+
+template <typename T> __device__ __forceinline__ SliceSmem<T> slice_smem(unsigned char* raw, int M, int nj) {
+    constexpr int TILE = PointTile<T>::value;
+    SliceSmem<T> m;
+    m.sa = reinterpret_cast<T*>(raw);
+    m.sc = m.sa + (size_t)M * TILE;
+    m.jval = m.sc + (size_t)M * TILE;
+    m.jptr = reinterpret_cast<int*>(m.jval + nj);
+    m.jrow = reinterpret_cast<int16_t*>(m.jptr + 6);
+    m.jcol = m.jrow + nj;
+    return m;
+}
+
+template <typename T> __device__ __forceinline__ void stage_jlists(const JLists& jl, const SliceSmem<T>& m) {
+    for (int e = threadIdx.x; e < jl.n; e += blockDim.x) {
+        m.jval[e] = (T)jl.val[e];
+        m.jrow[e] = jl.row[e];
+        m.jcol[e] = jl.col[e];
+    }
+    for (int e = threadIdx.x; e < 6; e += blockDim.x) m.jptr[e] = jl.ptr[e];
+}
+
+// stage the coefficient vectors of one slice for the tile's points (zeros
+// past the end of the grid)
 template <typename T>
-__global__ void stensor_accum(const T* __restrict__ qf, const T* __restrict__ qb, DensityArgs d, JLists jl,
-                              double* __restrict__ sraw) {
-    const int64_t nr = d.nr;
-    const int64_t sl = (int64_t)d.M * nr;
-    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x) {
-        for (int b = 0; b < 3; ++b) {
-            double acc[5] = {0, 0, 0, 0, 0};
-            const int s0 = d.nstart[b], n = d.ns[b];
-            if (n > 0) {
-                for (int s = s0; s <= s0 + n; ++s) {
-                    const int j = s - s0;
-                    const double wgt = (j == 0 || j == n) ? 1.0 : ((j & 1) ? 4.0 : 2.0);
-                    const T* a = qf + s * sl + r;
-                    const T* c = qb + s * sl + r;
-                    for (int t = 0; t < 5; ++t) {
-                        double sum = 0.0;
-                        for (int e = jl.ptr[t]; e < jl.ptr[t + 1]; ++e)
-                            sum += jl.val[e] * (double)a[(int64_t)jl.row[e] * nr] * (double)c[(int64_t)jl.col[e] * nr];
-                        acc[t] += wgt * sum;
-                    }
-                }
-            }
-            for (int t = 0; t < 5; ++t) sraw[((int64_t)b * 5 + t) * nr + r] = acc[t] * d.ds / 3.0;
-        }
+__device__ __forceinline__ void stage_tile(const T* __restrict__ a, const T* __restrict__ c, int M, int64_t nr,
+                                           int64_t r0, T* sa, T* sc) {
+    constexpr int TILE = PointTile<T>::value;
+    for (int idx = threadIdx.x; idx < M * TILE; idx += blockDim.x) {
+        const int i = idx / TILE, k = idx % TILE;
+        const int64_t r = r0 + k;
+        const bool ok = r < nr;
+        sa[idx] = ok ? a[(int64_t)i * nr + r] : (T)0;
+        sc[idx] = ok ? c[(int64_t)i * nr + r] : (T)0;
     }
 }
 
+// q^T J_t q* at one point from staged vectors (stride TILE) and staged lists
+template <typename T> __device__ __forceinline__ double jt_form(const SliceSmem<T>& m, int t, int k) {
+    constexpr int TILE = PointTile<T>::value;
+    T v = (T)0;
+    for (int e = m.jptr[t]; e < m.jptr[t + 1]; ++e) v += m.jval[e] * m.sa[m.jrow[e] * TILE + k] * m.sc[m.jcol[e] * TILE + k];
+    return (double)v;
+}
+
+// orientation tensor per block (SCFT_Density_FE.f90:161-220):
+// sraw[b][t][r] = S1_s( q^T J_t q* ), t = 11, 22, 12, 13, 23; thread (k, t)
 template <typename T>
-__device__ __forceinline__ void density_slice_body(const T* __restrict__ a, const T* __restrict__ c,
-                                                   const DensityArgs& d, int s, int want_s, const JLists& jl,
-                                                   double* __restrict__ raw, double* __restrict__ junc,
-                                                   double* __restrict__ qend, double* __restrict__ sraw,
-                                                   int64_t r0, int64_t rstep) {
+__global__ void __launch_bounds__(PointTile<T>::value * kSGroups)
+    stensor_accum(const T* __restrict__ qf, const T* __restrict__ qb, DensityArgs d, JLists jl,
+                  double* __restrict__ sraw) {
+    constexpr int TILE = PointTile<T>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const SliceSmem<T> m = slice_smem<T>(smem_raw, d.M, jl.n);
+    stage_jlists(jl, m);
+    const int64_t nr = d.nr;
+    const int64_t sl = (int64_t)d.M * nr;
+    const int k = threadIdx.x % TILE, t = threadIdx.x / TILE;
+    const int64_t r0 = (int64_t)blockIdx.x * TILE, r = r0 + k;
+    double acc[3] = {0.0, 0.0, 0.0};
+    for (int b = 0; b < 3; ++b) {
+        const int s0 = d.nstart[b], n = d.ns[b];
+        if (n <= 0) continue;
+        for (int s = s0; s <= s0 + n; ++s) {
+            const int j = s - s0;
+            const double wgt = (j == 0 || j == n) ? 1.0 : ((j & 1) ? 4.0 : 2.0);
+            __syncthreads();
+            stage_tile(qf + s * sl, qb + s * sl, d.M, nr, r0, m.sa, m.sc);
+            __syncthreads();
+            acc[b] += wgt * jt_form(m, t, k);
+        }
+    }
+    if (r < nr)
+        for (int b = 0; b < 3; ++b) sraw[((int64_t)b * 5 + t) * nr + r] = acc[b] * d.ds / 3.0;
+}
+
+// Streamed form of density_accum / stensor_accum: one slice s per launch,
+// issued by the backward sweep right after q*(s) is computed (descending s),
+// so the q* slices need not be stored.  Same Simpson weights per block.  One
+// CTA per tile of points; the tile's coefficient vectors of q(s) and q*(s)
+// are staged in shared memory once.
+// One CTA walks tiles of TILE points of one instance; thread (k, g): point k,
+// group g (g = 0 the densities, g = t the tensor component t when want_s;
+// blockDim = TILE * kSGroups when any instance of the launch wants S).
+template <typename T>
+__device__ __forceinline__ void density_slice_tiles(const T* __restrict__ a, const T* __restrict__ c,
+                                                    const DensityArgs& d, int s, int want_s, const JLists& jl,
+                                                    double* __restrict__ raw, double* __restrict__ junc,
+                                                    double* __restrict__ qend, double* __restrict__ sraw) {
+    constexpr int TILE = PointTile<T>::value;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const SliceSmem<T> m = slice_smem<T>(smem_raw, d.M, want_s ? jl.n : 0);
+    if (want_s) stage_jlists(jl, m);
     const int64_t nr = d.nr;
     double wgt[3];
     bool any = false;
@@ -201,50 +308,51 @@ __device__ __forceinline__ void density_slice_body(const T* __restrict__ a, cons
         }
     }
     const int sj[3] = {d.nstart[1], d.nstart[2], d.nmax};
-    const bool last = s == 0;
-    const double sc = d.ds / 3.0;
-    for (int64_t r = r0; r < nr; r += rstep) {
-        const double sum = dot_coeffs(a + r, c + r, d.M, nr);
-        if (any)
-            for (int b = 0; b < 3; ++b)
-                if (wgt[b] != 0.0) raw[b * nr + r] += wgt[b] * sum;
-        for (int j = 0; j < 3; ++j)
-            if (s == sj[j]) junc[j * nr + r] = sum;
-        if (s == d.nmax) qend[r] = (double)a[r];
-        if (want_s && any) {
-            for (int t = 0; t < 5; ++t) {
-                double st = 0.0;
-                for (int e = jl.ptr[t]; e < jl.ptr[t + 1]; ++e)
-                    st += jl.val[e] * (double)a[(int64_t)jl.row[e] * nr + r] * (double)c[(int64_t)jl.col[e] * nr + r];
+    const double scl = d.ds / 3.0;
+    const int k = threadIdx.x % TILE, g = threadIdx.x / TILE;
+    for (int64_t r0 = (int64_t)blockIdx.x * TILE; r0 < nr; r0 += (int64_t)gridDim.x * TILE) {
+        __syncthreads();  // lists staged / previous tile consumed
+        stage_tile(a, c, d.M, nr, r0, m.sa, m.sc);
+        __syncthreads();
+        const int64_t r = r0 + k;
+        if (r >= nr) continue;
+        if (g == 0) {
+            const double sum = dot_coeffs(m.sa + k, m.sc + k, d.M, (int64_t)TILE);
+            if (any)
                 for (int b = 0; b < 3; ++b)
-                    if (wgt[b] != 0.0) sraw[((int64_t)b * 5 + t) * nr + r] += wgt[b] * st;
-            }
+                    if (wgt[b] != 0.0) raw[b * nr + r] += wgt[b] * sum;
+            for (int j = 0; j < 3; ++j)
+                if (s == sj[j]) junc[j * nr + r] = sum;
+            if (s == d.nmax) qend[r] = (double)a[r];
+            if (s == 0)  // last slice of the backward sweep
+                for (int b = 0; b < 3; ++b) raw[b * nr + r] *= scl;
         }
-        if (last) {
-            for (int b = 0; b < 3; ++b) raw[b * nr + r] *= sc;
-            if (want_s)
-                for (int q = 0; q < 15; ++q) sraw[(int64_t)q * nr + r] *= sc;
+        if (want_s && g < 5) {
+            if (any) {
+                const double st = jt_form(m, g, k);
+                for (int b = 0; b < 3; ++b)
+                    if (wgt[b] != 0.0) sraw[((int64_t)b * 5 + g) * nr + r] += wgt[b] * st;
+            }
+            if (s == 0)
+                for (int b = 0; b < 3; ++b) sraw[((int64_t)b * 5 + g) * nr + r] *= scl;
         }
     }
 }
 
-// Streamed form of density_accum / stensor_accum: one slice s per launch,
-// issued by the backward sweep right after q*(s) is computed (descending s),
-// so the q* slices need not be stored.  Same Simpson weights per block.
 template <typename T>
-__global__ void density_slice(const T* __restrict__ a, const T* __restrict__ c, DensityArgs d, int s, int want_s,
-                              JLists jl, double* __restrict__ raw, double* __restrict__ junc,
-                              double* __restrict__ qend, double* __restrict__ sraw) {
-    density_slice_body<T>(a, c, d, s, want_s, jl, raw, junc, qend, sraw,
-                          blockIdx.x * (int64_t)blockDim.x + threadIdx.x, (int64_t)gridDim.x * blockDim.x);
+__global__ void __launch_bounds__(PointTile<T>::value * kSGroups)
+    density_slice(const T* __restrict__ a, const T* __restrict__ c, DensityArgs d, int s, int want_s, JLists jl,
+                  double* __restrict__ raw, double* __restrict__ junc, double* __restrict__ qend,
+                  double* __restrict__ sraw) {
+    density_slice_tiles<T>(a, c, d, s, want_s, jl, raw, junc, qend, sraw);
 }
 
 template <typename T>
-__global__ void density_slice_batched(const SliceBatchArgs<T>* __restrict__ args, int s) {
+__global__ void __launch_bounds__(PointTile<T>::value * kSGroups)
+    density_slice_batched(const SliceBatchArgs<T>* __restrict__ args, int s) {
     const SliceBatchArgs<T> g = args[blockIdx.y];
-    density_slice_body<T>(g.qf + (int64_t)s * g.sl, g.qb + (int64_t)(s & 3) * g.sl, g.d, s, g.want_s, g.jl, g.raw,
-                          g.junc, g.qend, g.sraw, blockIdx.x * (int64_t)blockDim.x + threadIdx.x,
-                          (int64_t)gridDim.x * blockDim.x);
+    density_slice_tiles<T>(g.qf + (int64_t)s * g.sl, g.qb + (int64_t)(s & 3) * g.sl, g.d, s, g.want_s, g.jl, g.raw,
+                           g.junc, g.qend, g.sraw);
 }
 
 // periodic Simpson weight product (utility_mod.f90:236-298): (h/3)*(2|4)
@@ -340,10 +448,19 @@ template <typename T> void launch_set_delta(T* q, int M, int64_t nr, cudaStream_
 template <typename T> void launch_make_cf(const double* w, T* cf, double ds, double third, int64_t nr, cudaStream_t st) {
     make_cf<T><<<grid_for(nr), 256, 0, st>>>(w, cf, ds, third, nr);
 }
+// CTAs of the tiled kernels: enough to fill the GPU, each walking several
+// tiles so that the staged lists are reused
+static unsigned tile_grid(int64_t nr, int tile) {
+    const int64_t tiles = (nr + tile - 1) / tile;
+    return (unsigned)(tiles < 1216 ? (tiles < 1 ? 1 : tiles) : 1216);
+}
+
 template <typename T>
 void launch_ms_term(const T* h1, const T* h2, const T* h3, int order, const double* mop, const ThetaLists& tl,
                     double ds, double thresh, int M, int64_t nr, T* out, cudaStream_t st) {
-    ms_term<T><<<grid_for(nr), 128, 0, st>>>(h1, h2, h3, order, mop, tl, ds, thresh, M, nr, out);
+    constexpr int TILE = PointTile<T>::value;
+    ms_term<T><<<tile_grid(nr, TILE), TILE * kMsGroups, ms_smem_bytes<T>(tl.n, M), st>>>(h1, h2, h3, order, mop, tl,
+                                                                                      ds, thresh, M, nr, out);
 }
 template <typename T>
 void launch_density(const T* qf, const T* qb, const DensityArgs& d, double* raw, double* junc, double* qend,
@@ -352,18 +469,26 @@ void launch_density(const T* qf, const T* qb, const DensityArgs& d, double* raw,
 }
 template <typename T>
 void launch_stensor(const T* qf, const T* qb, const DensityArgs& d, const JLists& jl, double* sraw, cudaStream_t st) {
-    stensor_accum<T><<<grid_for(d.nr), 128, 0, st>>>(qf, qb, d, jl, sraw);
+    constexpr int TILE = PointTile<T>::value;
+    stensor_accum<T><<<(unsigned)((d.nr + TILE - 1) / TILE), TILE * kSGroups, slice_smem_bytes<T>(d.M, jl.n, true),
+                       st>>>(qf, qb, d, jl, sraw);
 }
 
 template <typename T>
 void launch_density_slice(const T* qf_s, const T* qb_s, const DensityArgs& d, int s, int want_s, const JLists& jl,
                           double* raw, double* junc, double* qend, double* sraw, cudaStream_t st) {
-    density_slice<T><<<grid_for(d.nr), 256, 0, st>>>(qf_s, qb_s, d, s, want_s, jl, raw, junc, qend, sraw);
+    constexpr int TILE = PointTile<T>::value;
+    density_slice<T><<<tile_grid(d.nr, TILE), TILE * (want_s ? kSGroups : 1),
+                       slice_smem_bytes<T>(d.M, jl.n, want_s != 0), st>>>(qf_s, qb_s, d, s, want_s, jl, raw, junc,
+                                                                          qend, sraw);
 }
 
 template <typename T>
-void launch_density_slice_batched(const SliceBatchArgs<T>* args, int count, int64_t max_nr, int s, cudaStream_t st) {
-    density_slice_batched<T><<<dim3(grid_for(max_nr), count), 256, 0, st>>>(args, s);
+void launch_density_slice_batched(const SliceBatchArgs<T>* args, int count, int64_t max_nr, int s, int M, int nj,
+                                  int any_s, cudaStream_t st) {
+    constexpr int TILE = PointTile<T>::value;
+    density_slice_batched<T><<<dim3(tile_grid(max_nr, TILE), count), TILE * (any_s ? kSGroups : 1),
+                               slice_smem_bytes<T>(M, nj, any_s != 0), st>>>(args, s);
 }
 
 void launch_s3(const double* a, int nsum, int64_t stride, const S3Args& s, double* part, double* out,
@@ -396,9 +521,25 @@ void launch_nonfinite(const double* a, int64_t n, int* flag, cudaStream_t st) {
     template void launch_stensor<T>(const T*, const T*, const DensityArgs&, const JLists&, double*, cudaStream_t); \
     template void launch_density_slice<T>(const T*, const T*, const DensityArgs&, int, int, const JLists&, double*, \
                                           double*, double*, double*, cudaStream_t);                              \
-    template void launch_density_slice_batched<T>(const SliceBatchArgs<T>*, int, int64_t, int, cudaStream_t);
+    template void launch_density_slice_batched<T>(const SliceBatchArgs<T>*, int, int64_t, int, int, int, int,        \
+                                                  cudaStream_t);
 WLC_INST(double)
 WLC_INST(float)
 #undef WLC_INST
+
+void prepare_reduce_kernels() {
+    static bool done = false;
+    if (done) return;
+    const int big = 200 * 1024;
+    cudaFuncSetAttribute(stensor_accum<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(stensor_accum<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(density_slice<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(density_slice<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(density_slice_batched<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(density_slice_batched<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(ms_term<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    cudaFuncSetAttribute(ms_term<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
+    done = true;
+}
 
 }  // namespace wlc

@@ -32,6 +32,7 @@ struct FeArgs {
 // values val[5e + c], c = T1122, T33, T12, T13, T23
 struct ThetaLists {
     int n;
+    const int* rowptr;  // [M+1]: entries of row i at [rowptr[i], rowptr[i+1]) (entries are sorted by row)
     const int16_t* row;
     const int16_t* col;
     const double* val;
@@ -39,11 +40,24 @@ struct ThetaLists {
 
 // five J lists (J11, J22, J12, J13, J23) concatenated; ptr[6]
 struct JLists {
+    int n;  // total entries (ptr[5])
     const int* ptr;
     const int16_t* row;
     const int16_t* col;
     const double* val;
 };
+
+// points per CTA of the tiled per-point coefficient kernels (ms_term,
+// density slices, orientation tensor): the coefficient vectors of the tile
+// are staged in shared memory once
+template <typename T> struct PointTile {
+    static constexpr int value = sizeof(T) == 8 ? 32 : 64;
+};
+// function attributes of the tiled kernels (large shared memory); call once
+// per process before any stream capture
+void prepare_reduce_kernels();
+constexpr int kMsGroups = 4;  // ms_term: row groups per point (threads per point)
+constexpr int kSGroups = 5;   // orientation tensor: one thread per component per point
 
 template <typename T> void launch_to_internal(const double* ref, T* out, int M, int64_t nr, cudaStream_t st);
 template <typename T> void launch_to_reference(const T* in, double* ref, int M, int64_t nr, cudaStream_t st);
@@ -76,7 +90,8 @@ template <typename T> struct SliceBatchArgs {
     double* sraw;
 };
 template <typename T>
-void launch_density_slice_batched(const SliceBatchArgs<T>* args, int count, int64_t max_nr, int s, cudaStream_t st);
+void launch_density_slice_batched(const SliceBatchArgs<T>* args, int count, int64_t max_nr, int s, int M, int nj,
+                                  int any_s, cudaStream_t st);
 
 template <typename T>
 void launch_density_slice(const T* qf_s, const T* qb_s, const DensityArgs& d, int s, int want_s, const JLists& jl,
