@@ -273,6 +273,31 @@ int wlc_io_append_free_energy(const char* path, int32_t n_iter, double fe, doubl
                               const double* chi, const int32_t* ns, int32_t nmax);
 int wlc_io_append_errors(const char* path, int32_t n_iter, const double* err, int32_t nerr);
 
+/* No counterpart in the reference.  Learned warm start of the field
+ * iteration: a 3D convolutional encoder-decoder (periodic padding; grid
+ * levels G, G/2, G/4, G/8; widths C, 2C, 4C; skip connections) mapping six
+ * input channels on a G^3 grid (a noise field and five instance parameters
+ * as constant fields) to three output fields (the normalised block fields).
+ * BF16 weights and activations, FP32 accumulation on the tensor cores, FP32
+ * Adam; forward, backward and training all run on the device.
+ * Layouts: input [6][G^3], output / target [3][G^3] (channel, then point
+ * x + G(y + Gz)).  grid: multiple of 8 in [8, 64]; width: multiple of 16 in
+ * [16, 64]; seed: weight initialisation. */
+typedef struct wlc_net wlc_net;
+int wlc_net_create(int32_t grid, int32_t width, uint64_t seed, wlc_net** out);
+int wlc_net_destroy(wlc_net* net);
+const char* wlc_net_last_error(const wlc_net* net);
+int64_t wlc_net_param_count(const wlc_net* net);
+/* FP32 master parameters: per layer (e1..e6, d1..d3, out) W[27][ci][co] then b[co] */
+int wlc_net_get_params(const wlc_net* net, float* params);
+int wlc_net_set_params(wlc_net* net, const float* params);
+int wlc_net_forward(wlc_net* net, const float* input, float* output);
+/* mean-squared-error loss of one sample and its gradient w.r.t. the parameters (grad may be NULL) */
+int wlc_net_loss_grad(wlc_net* net, const float* input, const float* target, double* loss, float* grad);
+/* Adam training: inputs [n][6][G^3], targets [n][3][G^3]; loss_hist[epochs] (may be NULL) */
+int wlc_net_train(wlc_net* net, const float* inputs, const float* targets, int32_t nsamples, int32_t batch,
+                  int32_t epochs, float lr, uint64_t seed, double* loss_hist);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,7 +39,9 @@ SYMBOLS = ["wlc_abi_version", "wlc_create", "wlc_destroy", "wlc_last_error", "wl
            "wlc_batch_destroy", "wlc_batch_last_error", "wlc_batch_size", "wlc_batch_groups", "wlc_batch_get",
            "wlc_batch_propagate", "wlc_batch_autotune", "wlc_batch_use_graph", "wlc_batch_stream",
            "wlc_batch_launch_count", "wlc_io_write_w", "wlc_io_read_w", "wlc_io_write_mop", "wlc_io_read_mop",
-           "wlc_io_write_rho", "wlc_io_append_free_energy", "wlc_io_append_errors"]
+           "wlc_io_write_rho", "wlc_io_append_free_energy", "wlc_io_append_errors", "wlc_net_create",
+           "wlc_net_destroy", "wlc_net_last_error", "wlc_net_param_count", "wlc_net_get_params",
+           "wlc_net_set_params", "wlc_net_forward", "wlc_net_loss_grad", "wlc_net_train"]
 
 
 class WlcError(RuntimeError):
@@ -128,6 +130,18 @@ def load(build_if_missing=True):
     lib.wlc_io_write_rho.argtypes = [C, Dp, ctypes.POINTER(ctypes.c_int32), Dp]
     lib.wlc_io_append_free_energy.argtypes = [C, I, D, D, D, Dp, ctypes.POINTER(ctypes.c_int32), I]
     lib.wlc_io_append_errors.argtypes = [C, I, Dp, I]
+    Fp = ctypes.POINTER(ctypes.c_float)
+    lib.wlc_net_create.argtypes = [I, I, ctypes.c_uint64, ctypes.POINTER(P)]
+    lib.wlc_net_destroy.argtypes = [P]
+    lib.wlc_net_last_error.argtypes = [P]
+    lib.wlc_net_last_error.restype = ctypes.c_char_p
+    lib.wlc_net_param_count.argtypes = [P]
+    lib.wlc_net_param_count.restype = ctypes.c_int64
+    lib.wlc_net_get_params.argtypes = [P, Fp]
+    lib.wlc_net_set_params.argtypes = [P, Fp]
+    lib.wlc_net_forward.argtypes = [P, Fp, Fp]
+    lib.wlc_net_loss_grad.argtypes = [P, Fp, Fp, Dp, Fp]
+    lib.wlc_net_train.argtypes = [P, Fp, Fp, I, I, I, ctypes.c_float, ctypes.c_uint64, Dp]
     Ip = ctypes.POINTER(ctypes.c_int32)
     lib.wlc_autotune.argtypes = [P, Ip]
     lib.wlc_set_launch_config.argtypes = [P, I, I]
@@ -537,3 +551,77 @@ class io:
     def append_errors(path, n_iter, err):
         e = np.ascontiguousarray(err, dtype=np.float64).reshape(-1)
         io._rc(load().wlc_io_append_errors(os.fsencode(path), int(n_iter), _dp(e), len(e)), "append " + str(path))
+
+
+def _fp(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class WarmStartNet:
+    """Learned warm start (wlc_net_*): a 3D conv encoder-decoder on a G^3
+    grid, BF16 tensor-core kernels with FP32 accumulation, trained on the
+    device.  Input (6, G^3): a noise field and five instance parameters as
+    constant fields; output (3, G^3): normalised block fields."""
+
+    def __init__(self, grid=32, width=32, seed=1):
+        self.lib = load()
+        self.G, self.C = int(grid), int(width)
+        self.h = ctypes.c_void_p()
+        rc = self.lib.wlc_net_create(self.G, self.C, int(seed), ctypes.byref(self.h))
+        if rc != 0:
+            msg = self.lib.wlc_net_last_error(self.h).decode() if self.h else ""
+            self.lib.wlc_net_destroy(self.h)
+            self.h = None
+            raise WlcError(rc, msg)
+        self.np = self.lib.wlc_net_param_count(self.h)
+
+    def _check(self, rc):
+        if rc != 0:
+            raise WlcError(rc, self.lib.wlc_net_last_error(self.h).decode())
+
+    @property
+    def npts(self):
+        return self.G ** 3
+
+    def params(self):
+        p = np.empty(self.np, dtype=np.float32)
+        self._check(self.lib.wlc_net_get_params(self.h, _fp(p)))
+        return p
+
+    def set_params(self, p):
+        p = np.ascontiguousarray(p, dtype=np.float32).reshape(self.np)
+        self._check(self.lib.wlc_net_set_params(self.h, _fp(p)))
+
+    def forward(self, x):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(6, self.npts)
+        out = np.empty((3, self.npts), dtype=np.float32)
+        self._check(self.lib.wlc_net_forward(self.h, _fp(x), _fp(out)))
+        return out
+
+    def loss_grad(self, x, t):
+        x = np.ascontiguousarray(x, dtype=np.float32).reshape(6, self.npts)
+        t = np.ascontiguousarray(t, dtype=np.float32).reshape(3, self.npts)
+        loss = np.zeros(1)
+        g = np.empty(self.np, dtype=np.float32)
+        self._check(self.lib.wlc_net_loss_grad(self.h, _fp(x), _fp(t), _dp(loss), _fp(g)))
+        return float(loss[0]), g
+
+    def train(self, inputs, targets, batch=8, epochs=10, lr=1e-3, seed=7):
+        x = np.ascontiguousarray(inputs, dtype=np.float32)
+        t = np.ascontiguousarray(targets, dtype=np.float32)
+        n = x.shape[0]
+        hist = np.zeros(epochs)
+        self._check(self.lib.wlc_net_train(self.h, _fp(x.reshape(-1)), _fp(t.reshape(-1)), n, int(batch),
+                                           int(epochs), float(lr), int(seed), _dp(hist)))
+        return hist
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.wlc_net_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
