@@ -647,6 +647,148 @@ def run_large(args):
     inst.close()
 
 
+WS_G, WS_NMAX, WS_L = 32, 100, 6
+
+
+def ws_draws(count, seed):
+    """Instance parameters of the warm-start data set (the batched sweep's
+    ranges): fA, fC ~ U(0.2, 0.4), chiN ~ U(12, 24), L/lp ~ U(0.5, 3.0),
+    box 4.0 Rg; and the 16^3 noise seed of each instance."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        out.append(dict(fa=rng.uniform(0.2, 0.4), fc=rng.uniform(0.2, 0.4), chi=rng.uniform(12.0, 24.0),
+                        x=rng.uniform(0.5, 3.0), noise_seed=int(rng.integers(1 << 31))))
+    return out
+
+
+def ws_noise(seed):
+    """16^3 N(0, 1) noise, nearest-upsampled to the 32^3 grid."""
+    xi = np.random.default_rng(seed).normal(size=(16, 16, 16))  # [z][y][x]
+    return xi.repeat(2, 0).repeat(2, 1).repeat(2, 2).reshape(-1)
+
+
+def ws_spec(d):
+    import wlc
+    box = 4.0 * wlc.wlc_radius_of_gyration(d["x"])
+    return dict(n=WS_G, lmax=WS_L, nmax=WS_NMAX, ns=wlc.even_block_lengths((d["fa"], 1 - d["fa"] - d["fc"], d["fc"]),
+                                                                          WS_NMAX),
+                dx=box / WS_G, loa=d["x"] * 0.5, kappa=(0.5, 0.5, 0.5), chi=(d["chi"],) * 3)
+
+
+def ws_input(d):
+    """network input (6, G^3): the noise field and the five parameters
+    (scaled to about [-1, 1]) as constant fields"""
+    import wlc
+    box = 4.0 * wlc.wlc_radius_of_gyration(d["x"])
+    par = [(d["fa"] - 0.3) / 0.1, (d["fc"] - 0.3) / 0.1, (d["chi"] - 18.0) / 6.0, (d["x"] - 1.75) / 1.25,
+           box - 1.0]
+    P = WS_G ** 3
+    return np.concatenate([ws_noise(d["noise_seed"])[None, :], np.repeat(np.array(par)[:, None], P, axis=1)])
+
+
+def ws_cold(d):
+    xi = ws_noise(d["noise_seed"])
+    return 0.3 * np.stack([xi, -xi, np.zeros_like(xi)])
+
+
+def ws_solve(draws, w0s, iters, tol=0.0):
+    """SCFT of all draws together (one batch, FP32 propagators, field update
+    on the device) from the given fields; returns final fields and the
+    per-iteration max block residual of every instance."""
+    import wlc
+    b = wlc.Batch([ws_spec(d) for d in draws])
+    for inst, w0 in zip(b.instances, w0s):
+        inst.set_fields(w0)
+    b.autotune()
+    mp = wlc.mix_params(anderson_depth=5)
+    res = np.zeros((len(draws), iters))
+    fe = np.zeros((len(draws), iters))
+    done = np.zeros(len(draws), dtype=bool)
+    for it in range(iters):
+        b.propagate()
+        for j, inst in enumerate(b.instances):
+            inst.density(want_junction=False)
+            fe[j, it] = inst.free_energy()
+            err, conv = inst.iterate(mp)
+            res[j, it] = max(err[:3])
+        if tol > 0 and (res[:, it] < tol).all():
+            res, fe = res[:, :it + 1], fe[:, :it + 1]
+            break
+    ws = [inst.get_fields() for inst in b.instances]
+    b.close()
+    return ws, res, fe
+
+
+def run_warmstart(args):
+    """Learned warm start: solver-generated training fields (32^3, l <= 6,
+    Ns = 100, the batched sweep's parameter ranges, fields after
+    --ws-iters iterations from the cold start), network training on the
+    device, then warm vs cold starts on held-out draws."""
+    import torch
+    import wlc
+    t0 = time.perf_counter()
+    ntr, nte = args.ws_train, args.ws_test
+    draws = ws_draws(ntr + nte, 11)
+    train, test = draws[:ntr], draws[ntr:]
+    # training data: the solver's fields after ws_iters iterations
+    targets = []
+    chunk = 64
+    for c0 in range(0, ntr, chunk):
+        part = train[c0:c0 + chunk]
+        ws, _, _ = ws_solve(part, [ws_cold(d) for d in part], args.ws_iters)
+        for d, w in zip(part, ws):
+            targets.append((w - w.mean(axis=1, keepdims=True)) / d["chi"])
+    t_data = time.perf_counter() - t0
+    X = np.stack([ws_input(d) for d in train]).astype(np.float32)
+    T = np.stack(targets).astype(np.float32)
+    net = wlc.WarmStartNet(WS_G, 32, seed=1)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    hist = net.train(X, T, batch=8, epochs=args.ws_epochs, lr=args.ws_lr)
+    torch.cuda.synchronize()
+    t_train = time.perf_counter() - t1
+    # held-out draws: cold start vs the network's fields
+    Xte = np.stack([ws_input(d) for d in test]).astype(np.float32)
+    t2 = time.perf_counter()
+    warm0 = [net.forward(x).astype(np.float64) * d["chi"] for x, d in zip(Xte, test)]
+    t_pred = time.perf_counter() - t2
+    wc, res_c, fe_c = ws_solve(test, [ws_cold(d) for d in test], args.ws_eval_iters)
+    # held-out error of the network against the solver's fields after as many iterations
+    tt = [(w - w.mean(axis=1, keepdims=True)) / d["chi"] for w, d in zip(wc, test)]
+    test_mse = float(np.mean([np.mean((net.forward(x) - t) ** 2) for x, t in zip(Xte, tt)]))
+    test_var = float(np.mean([np.mean(t ** 2) for t in tt]))
+    _, res_w, fe_w = ws_solve(test, warm0, args.ws_eval_iters)
+
+    def first_below(res, thr):
+        out = []
+        for r in res:
+            k = np.nonzero(r < thr)[0]
+            out.append(int(k[0]) + 1 if k.size else None)
+        return out
+
+    summary = {}
+    for thr in (1e-1, 3e-2, 1e-2, 3e-3, 1e-3):
+        c, w = first_below(res_c, thr), first_below(res_w, thr)
+        both = [(a, b) for a, b in zip(c, w) if a is not None and b is not None]
+        summary["%g" % thr] = {"cold_reached": sum(a is not None for a in c), "warm_reached": sum(b is not None for b in w),
+                               "median_cold_iters": float(np.median([a for a, _ in both])) if both else None,
+                               "median_warm_iters": float(np.median([b for _, b in both])) if both else None}
+    line = {"metric": "learned warm start: iterations to a residual, warm vs cold (32^3, L=6, Ns=100)",
+            "train_instances": ntr, "test_instances": nte, "data_iterations": args.ws_iters,
+            "params": int(net.np), "epochs": args.ws_epochs, "lr": args.ws_lr,
+            "train_loss_first_last": [float(hist[0]), float(hist[-1])], "train_loss": [float(v) for v in hist],
+            "test_mse": test_mse, "test_target_mean_square": test_var,
+            "seconds": {"data": t_data, "train": t_train, "predict_all": t_pred},
+            "eval_iterations": args.ws_eval_iters, "thresholds": summary,
+            "median_final_residual": {"cold": float(np.median(res_c[:, -1])), "warm": float(np.median(res_w[:, -1]))},
+            "median_residual_at_50": {"cold": float(np.median(res_c[:, min(49, res_c.shape[1] - 1)])),
+                                      "warm": float(np.median(res_w[:, min(49, res_w.shape[1] - 1)]))},
+            "median_abs_F_diff_final": float(np.median(np.abs(fe_c[:, -1] - fe_w[:, -1])))}
+    print(json.dumps(line))
+    net.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -657,7 +799,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--profile", action="store_true", help="small-footprint case for ncu captures")
     ap.add_argument("--converge", action="store_true", help="time-to-converged F instead of steps/s")
-    ap.add_argument("--workload", default="single", choices=["single", "batch", "large"])
+    ap.add_argument("--workload", default="single", choices=["single", "batch", "large", "warmstart"])
+    ap.add_argument("--ws-train", type=int, default=128)
+    ap.add_argument("--ws-test", type=int, default=32)
+    ap.add_argument("--ws-iters", type=int, default=250)
+    ap.add_argument("--ws-epochs", type=int, default=40)
+    ap.add_argument("--ws-eval-iters", type=int, default=250)
+    ap.add_argument("--ws-lr", type=float, default=1e-4)
     ap.add_argument("--checkpoint", type=int, default=0, help="large workload: q checkpoint interval")
     ap.add_argument("--count", type=int, default=48, help="instances of the batched workload")
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration")
@@ -687,6 +835,9 @@ def main():
         return
     if args.workload == "large" and args.impl == "ours":
         run_large(args)
+        return
+    if args.workload == "warmstart" and args.impl == "ours":
+        run_warmstart(args)
         return
     wl = workload(args.precision)
     if args.impl == "reference":
