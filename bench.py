@@ -702,20 +702,25 @@ def ws_solve(draws, w0s, iters, tol=0.0):
         inst.set_fields(w0)
     b.autotune()
     mp = wlc.mix_params(anderson_depth=5)
-    res = np.zeros((len(draws), iters))
-    fe = np.zeros((len(draws), iters))
-    done = np.zeros(len(draws), dtype=bool)
+    res = np.full((len(draws), iters), np.nan)
+    fe = np.full((len(draws), iters), np.nan)
+    bad = np.zeros(len(draws), dtype=bool)  # iteration diverged (non-finite density): frozen
     for it in range(iters):
         b.propagate()
         for j, inst in enumerate(b.instances):
-            inst.density(want_junction=False)
-            fe[j, it] = inst.free_energy()
-            err, conv = inst.iterate(mp)
-            res[j, it] = max(err[:3])
-        if tol > 0 and (res[:, it] < tol).all():
+            if bad[j]:
+                continue
+            try:
+                inst.density(want_junction=False)
+                fe[j, it] = inst.free_energy()
+                err, conv = inst.iterate(mp)
+                res[j, it] = max(err[:3])
+            except wlc.WlcError:
+                bad[j] = True
+        if tol > 0 and (res[~bad, it] < tol).all():
             res, fe = res[:, :it + 1], fe[:, :it + 1]
             break
-    ws = [inst.get_fields() for inst in b.instances]
+    ws = [None if bad[j] else inst.get_fields() for j, inst in enumerate(b.instances)]
     b.close()
     return ws, res, fe
 
@@ -732,13 +737,18 @@ def run_warmstart(args):
     draws = ws_draws(ntr + nte, 11)
     train, test = draws[:ntr], draws[ntr:]
     # training data: the solver's fields after ws_iters iterations
-    targets = []
+    targets, kept = [], []
     chunk = 64
     for c0 in range(0, ntr, chunk):
         part = train[c0:c0 + chunk]
         ws, _, _ = ws_solve(part, [ws_cold(d) for d in part], args.ws_iters)
         for d, w in zip(part, ws):
+            if w is None or not np.isfinite(w).all():
+                continue
             targets.append((w - w.mean(axis=1, keepdims=True)) / d["chi"])
+            kept.append(d)
+    n_diverged_train = ntr - len(kept)
+    train = kept
     t_data = time.perf_counter() - t0
     X = np.stack([ws_input(d) for d in train]).astype(np.float32)
     T = np.stack(targets).astype(np.float32)
@@ -755,10 +765,15 @@ def run_warmstart(args):
     t_pred = time.perf_counter() - t2
     wc, res_c, fe_c = ws_solve(test, [ws_cold(d) for d in test], args.ws_eval_iters)
     # held-out error of the network against the solver's fields after as many iterations
-    tt = [(w - w.mean(axis=1, keepdims=True)) / d["chi"] for w, d in zip(wc, test)]
-    test_mse = float(np.mean([np.mean((net.forward(x) - t) ** 2) for x, t in zip(Xte, tt)]))
-    test_var = float(np.mean([np.mean(t ** 2) for t in tt]))
+    ok = [j for j, w in enumerate(wc) if w is not None and np.isfinite(w).all()]
+    tt = {j: (wc[j] - wc[j].mean(axis=1, keepdims=True)) / test[j]["chi"] for j in ok}
+    test_mse = float(np.mean([np.mean((net.forward(Xte[j]) - tt[j]) ** 2) for j in ok]))
+    test_var = float(np.mean([np.mean(tt[j] ** 2) for j in ok]))
     _, res_w, fe_w = ws_solve(test, warm0, args.ws_eval_iters)
+    both_ok = [j for j in range(len(test)) if np.isfinite(res_c[j, -1]) and np.isfinite(res_w[j, -1])]
+    n_div_cold = int(sum(not np.isfinite(res_c[j, -1]) for j in range(len(test))))
+    n_div_warm = int(sum(not np.isfinite(res_w[j, -1]) for j in range(len(test))))
+    res_c, res_w, fe_c, fe_w = res_c[both_ok], res_w[both_ok], fe_c[both_ok], fe_w[both_ok]
 
     def first_below(res, thr):
         out = []
@@ -775,7 +790,8 @@ def run_warmstart(args):
                                "median_cold_iters": float(np.median([a for a, _ in both])) if both else None,
                                "median_warm_iters": float(np.median([b for _, b in both])) if both else None}
     line = {"metric": "learned warm start: iterations to a residual, warm vs cold (32^3, L=6, Ns=100)",
-            "train_instances": ntr, "test_instances": nte, "data_iterations": args.ws_iters,
+            "train_instances": len(train), "train_diverged": n_diverged_train, "test_instances": nte,
+            "test_diverged": {"cold": n_div_cold, "warm": n_div_warm}, "data_iterations": args.ws_iters,
             "params": int(net.np), "epochs": args.ws_epochs, "lr": args.ws_lr,
             "train_loss_first_last": [float(hist[0]), float(hist[-1])], "train_loss": [float(v) for v in hist],
             "test_mse": test_mse, "test_target_mean_square": test_var,
