@@ -339,7 +339,8 @@ def run_ours(args, wl):
                                        "(400 contour steps)",
                            "precision": wl["precision"], "l2": "inputs larger than L2 (51 GB history/direction)",
                            "parallelism": "replicas" if world > 1 else "single",
-                           "launch_config": {"a_variant": tuned[0], "solve_threads": tuned[1]} if tuned else "default"},
+                           "launch_config": {"a_variant": tuned[0], "solve_threads": tuned[1],
+                                             "xy_threads": tuned[2]} if tuned else "default"},
                 "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
                 "wall_s": t_wall}
@@ -376,8 +377,7 @@ def run_profile_case(args):
     rng = np.random.default_rng(5)
     inst.set_fields(rng.normal(0.0, wl["w_sigma"], size=(3, wl["n"] ** 3)))
     if args.launch_config:
-        a_var, threads = (int(v) for v in args.launch_config.split(","))
-        inst.set_launch_config(a_var, threads)
+        inst.set_launch_config(*(int(v) for v in args.launch_config.split(",")))
     inst.MDE_q()
     inst.MDE_q()
     inst.MDE_qstar()
@@ -825,7 +825,7 @@ def main():
     ap.add_argument("--checkpoint", type=int, default=0, help="large workload: q checkpoint interval")
     ap.add_argument("--count", type=int, default=48, help="instances of the batched workload")
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration")
-    ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads")
+    ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads[,xy_threads]")
     ap.add_argument("--forms", default="fp32sched,fp64")
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--switch-tol", type=float, default=1e-4)

@@ -103,7 +103,7 @@ __device__ __forceinline__ void store_phat(const StepArgs<T>& a, const typename 
 
 // ---------------------------------------------------------------- pass A
 template <typename T, int N, bool B = false>
-__global__ void __launch_bounds__(256) rhs_fft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
+__global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
     const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
     constexpr int Z = zg_planes(N, sizeof(T));
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
 
 // ---------------------------------------------------------------- pass C
 template <typename T, int N, bool B = false>
-__global__ void __launch_bounds__(256) ifft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
+__global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
     const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
     constexpr int Z = zg_planes(N, sizeof(T));
@@ -296,6 +296,9 @@ template <typename T, int N, bool B> static void set_xy_attrs() {
     done = true;
 }
 
+// threads per CTA of the generic pass A and of pass C: 256 (default) or 512
+static inline int xy_block(int threads) { return threads == 512 ? 512 : 256; }
+
 // pass A variant: 0 = default (staged where it fits), 1 = generic, 2 = staged
 template <typename T, int N> static bool use_staged(int variant) {
     if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
@@ -316,12 +319,12 @@ template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s,
             staged = use_staged<T, N>(s.a_variant);
             if (staged) rhs_fft_xy_staged<N><<<gxy, 512, StagedA<N>::bytes, st>>>(s.step, nullptr);
         }
-        if (!staged) rhs_fft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step, nullptr);
+        if (!staged) rhs_fft_xy<T, N><<<gxy, xy_block(s.xy_threads), sxy, st>>>(s.step, nullptr);
     }
     if (s.events) cudaEventRecord(s.events[1], st);
     if (s.do_b) launch_solve<T>(N, s.solve, st, s.solve_threads);
     if (s.events) cudaEventRecord(s.events[2], st);
-    if (s.do_c) ifft_xy<T, N><<<gxy, 256, sxy, st>>>(s.step, nullptr);
+    if (s.do_c) ifft_xy<T, N><<<gxy, xy_block(s.xy_threads), sxy, st>>>(s.step, nullptr);
     if (s.events) cudaEventRecord(s.events[3], st);
     return cudaGetLastError();
 }
@@ -336,10 +339,10 @@ template <int N> static cudaError_t launch_batched_n(const BatchLaunch<float>& b
         staged = use_staged<float, N>(b.a_variant);
         if (staged) rhs_fft_xy_staged<N, true><<<gxy, 512, StagedA<N>::bytes, st>>>(StepArgs<float>{}, b.dstep);
     }
-    if (!staged) rhs_fft_xy<float, N, true><<<gxy, 256, sxy, st>>>(StepArgs<float>{}, b.dstep);
+    if (!staged) rhs_fft_xy<float, N, true><<<gxy, xy_block(b.xy_threads), sxy, st>>>(StepArgs<float>{}, b.dstep);
     cudaError_t e = launch_solve_batched(N, b, st);
     if (e != cudaSuccess) return e;
-    ifft_xy<float, N, true><<<gxy, 256, sxy, st>>>(StepArgs<float>{}, b.dstep);
+    ifft_xy<float, N, true><<<gxy, xy_block(b.xy_threads), sxy, st>>>(StepArgs<float>{}, b.dstep);
     return cudaGetLastError();
 }
 

@@ -17,6 +17,7 @@ template <typename T> struct StepLaunch {
     bool do_a = true, do_b = true, do_c = true;
     int a_variant = 0;      // pass A: 0 default, 1 generic, 2 staged (FP32, where it fits)
     int solve_threads = 0;  // pass B threads per CTA (0: default)
+    int xy_threads = 0;     // generic pass A and pass C threads per CTA (256 or 512; 0: 256)
     cudaEvent_t* events = nullptr;  // 4 events around the three passes, or null
 };
 
@@ -27,7 +28,7 @@ template <typename T> struct BatchLaunch {
     const SolveArgs<T>* dsolve = nullptr;
     int count = 0, M = 0, nkx = 0;
     size_t solve_smem = 0;
-    int a_variant = 0, solve_threads = 0;
+    int a_variant = 0, solve_threads = 0, xy_threads = 0;
 };
 
 template <typename T> cudaError_t launch_step(int N, const StepLaunch<T>& s, cudaStream_t st);
