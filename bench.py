@@ -317,9 +317,9 @@ def run_ours(args, wl):
     roofline = {"bound": "hbm", "kernel": pass_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                 "bytes_per_launch": pb[dom], "avg_launch_ms": avg_ms, "kernel_share": share,
-                "binding_limit": ("FP64 pipe: 74-80 % active in every pass (ncu, profiles/step_kernels_64c_L10_fp64.md);"
-                                  " the HBM fraction is reported as the contract asks") if bq == 8 else
-                                 "latency-bound shared-memory FFT stages (profiles/step_kernels_64c_L10_fp32.md)",
+                "binding_limit": ("FP64 pipe: 74-80 % active in every pass (ncu); the HBM fraction is"
+                                  " reported alongside") if bq == 8 else
+                                 "latency-bound shared-memory FFT stages (ncu: 8-18 % DRAM, ~10 % FMA pipe)",
                 "step": {"algorithmic_bytes": b_step, "ms": step_ms,
                          "achieved_gbs": b_step / (step_ms / 1000.0) / 1e9,
                          "frac": b_step / (step_ms / 1000.0) / 1e9 / peak}}

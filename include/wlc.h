@@ -6,7 +6,7 @@
  * module globals (global_parameters.f90:17-376) and has no bind(C) interface;
  * each entry point below replaces one reference routine (file:line cited) and
  * keeps that routine's meaning.  A Fortran host binds these through
- * ISO_C_BINDING (see INTEGRATION.md).
+ * ISO_C_BINDING.
  *
  * Conventions
  *  - Every function returns 0 on success or a negative WLC_E_* code;

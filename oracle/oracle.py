@@ -1,7 +1,7 @@
 """ctypes handle on the CPU FP64 oracle (oracle/wlc_oracle.c).
 
 TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and
-bench.py's cpu_baseline / reference leg, always as the checker.  The product
+bench.py's cpu_baseline / reference leg, always to test against.  The product
 library never imports it.
 
 The oracle restates the reference's arithmetic (file:line citations live in

@@ -1,5 +1,5 @@
 """CPU restatement of the SCFT field update -- TEST INFRASTRUCTURE ONLY
-(the checker for libwlc's wlc_iterate; imported by tests/ alone).
+(the oracle of libwlc's wlc_iterate; imported by tests/ alone).
 Parity unpinned: the reference has no two- or three-block golden vectors
 for the iteration.
 

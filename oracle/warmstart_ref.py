@@ -1,5 +1,5 @@
 """CPU restatement of the warm-start network (libwlc wlc_net_*) -- TEST
-INFRASTRUCTURE ONLY (the checker for the GPU forward / backward kernels;
+INFRASTRUCTURE ONLY (the oracle of the GPU forward / backward kernels;
 imported by tests/ alone).  The network has no counterpart in the
 reference.
 

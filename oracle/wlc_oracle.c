@@ -2,7 +2,7 @@
  * wlc_oracle.c -- CPU FP64 restatement of the wormlike-chain MDE hot path of
  * tjz2026/wormlike-chain-triblock (Fortran 90, MPI/FFTW/MKL).
  *
- * TEST INFRASTRUCTURE ONLY.  This file is the checker: only tests/,
+ * TEST INFRASTRUCTURE ONLY.  This file is the oracle: only tests/,
  * __graft_entry__.smoke() and bench.py's cpu_baseline / reference leg load it.
  * The product (libwlc, CUDA sm_103a) never links or calls it.
  *
