@@ -219,12 +219,14 @@ int wlc_last_timing(const wlc_ctx* ctx, double* ms4);
  * launch configurations of one contour step on this context's own data
  * (pass A variant, threads per solve CTA; all give identical results) and
  * keep the fastest.  Runs a forward sweep first if none is current.
- * config (may be NULL) receives {a_variant, solve_threads, xy_threads}
- * (pass A variant 1 generic / 2 staged; threads per solve CTA; threads per
- * CTA of the generic pass A and pass C, 256 or 512).
- * wlc_set_launch_config sets them by hand (0, 0, 0 = defaults). */
+ * config (may be NULL) receives {a_variant, solve_threads, xy_threads,
+ * xy_half_planes} (pass A variant 1 generic / 2 staged; threads per solve
+ * CTA; threads per CTA of the generic pass A and pass C, 256 or 512; 1 when
+ * those CTAs take half the default number of z planes).
+ * wlc_set_launch_config sets them by hand (0, 0, 0, 0 = defaults). */
 int wlc_autotune(wlc_ctx* ctx, int32_t* config);
-int wlc_set_launch_config(wlc_ctx* ctx, int32_t a_variant, int32_t solve_threads, int32_t xy_threads);
+int wlc_set_launch_config(wlc_ctx* ctx, int32_t a_variant, int32_t solve_threads, int32_t xy_threads,
+                          int32_t xy_half_planes);
 
 /* No counterpart in the reference (one instance per MPI job there).
  * Batches: independent FP32 instances (own grid, box, composition, chi,
@@ -247,7 +249,8 @@ int wlc_batch_get(wlc_batch* b, int32_t i, wlc_ctx** ctx);
 /* MDE_q and MDE_qstar of every instance (wormlike_MDE_2dcomp_mod.f90:231-1557
  * per instance); the graph is re-captured after a box or Maier-Saupe change. */
 int wlc_batch_propagate(wlc_batch* b);
-/* per grid-size group: config[4g..4g+3] = {N, a_variant, solve_threads, xy_threads} (may be NULL) */
+/* per grid-size group: config[5g..5g+4] = {N, a_variant, solve_threads, xy_threads, xy_half_planes}
+ * (may be NULL) */
 int wlc_batch_autotune(wlc_batch* b, int32_t* config);
 int wlc_batch_use_graph(wlc_batch* b, int32_t on);  /* 0: issue the launches directly */
 void* wlc_batch_stream(const wlc_batch* b);

@@ -59,7 +59,7 @@ struct wlc_ctx {
     bool stream = false;
     bool own_stream = true;   // false: the stream belongs to a batch
     bool batch_owned = false;
-    int a_variant = 0, solve_threads = 0, xy_threads = 0;  // launch configuration (autotuned or default)
+    int a_variant = 0, solve_threads = 0, xy_threads = 0, xy_z = 0;  // launch configuration (autotuned or default)
     void* phat = nullptr;
     void* cf = nullptr;
     void* work = nullptr;    // [M][nr] compute type: RHS / one-step scratch
@@ -621,6 +621,7 @@ static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h
     L.a_variant = c->a_variant;
     L.solve_threads = c->solve_threads;
     L.xy_threads = c->xy_threads;
+    L.xy_z = c->xy_z;
     const size_t nr = (size_t)c->nr;
     StepArgs<T>& a = L.step;
     a.h1 = h1;
@@ -1248,8 +1249,9 @@ template <typename T> static int autotune_impl(wlc_ctx* c) {
     auto at = [&](int q) -> T* { return c->K ? qf_ring<T>(c, q) : (T*)c->qf + (size_t)q * sl; };
     StepKind k{3, 1, blk_fwd(c, s)};
     float best = 1e30f;
-    int best_a = c->a_variant, best_t = c->solve_threads, best_x = c->xy_threads;
+    int best_a = c->a_variant, best_t = c->solve_threads, best_x = c->xy_threads, best_z = c->xy_z;
     const bool ms = std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop;
+    for (int xz : {0, 1})
     for (int xt : {256, 512})
     for (int av : {1, 2}) {
         if (av == 2 && sizeof(T) != 4) continue;
@@ -1257,6 +1259,7 @@ template <typename T> static int autotune_impl(wlc_ctx* c) {
             c->a_variant = av;
             c->solve_threads = th;
             c->xy_threads = xt;
+            c->xy_z = xz;
             StepLaunch<T> L = make_launch<T>(c, k, at(s - 1), at(s - 2), at(s - 3), at(s));
             if (ms) {  // the Theta term of this step (the buffer holds the last step of the last sweep)
                 launch_ms_term<T>(at(s - 1), at(s - 2), at(s - 3), 3, c->mop, c->thl, c->ds, lit_thresh(c->real4),
@@ -1271,12 +1274,14 @@ template <typename T> static int autotune_impl(wlc_ctx* c) {
                 best_a = av;
                 best_t = th;
                 best_x = xt;
+                best_z = xz;
             }
         }
     }
     c->a_variant = best_a;
     c->solve_threads = best_t;
     c->xy_threads = best_x;
+    c->xy_z = best_z;
     return WLC_OK;
 }
 
@@ -1289,15 +1294,19 @@ extern "C" int wlc_autotune(wlc_ctx* c, int32_t* config) {
         config[0] = c->a_variant;
         config[1] = c->solve_threads;
         config[2] = c->xy_threads;
+        config[3] = c->xy_z;
     }
     return WLC_OK;
 }
 
-extern "C" int wlc_set_launch_config(wlc_ctx* c, int32_t a_variant, int32_t solve_threads, int32_t xy_threads) {
+extern "C" int wlc_set_launch_config(wlc_ctx* c, int32_t a_variant, int32_t solve_threads, int32_t xy_threads,
+                                     int32_t xy_half_planes) {
     if (!ready(c)) return WLC_E_STATE;
     if (a_variant < 0 || a_variant > 2 || solve_threads < 0 || solve_threads > kSolveThreads ||
-        (xy_threads != 0 && xy_threads != 256 && xy_threads != 512))
-        return set_err(c, WLC_E_PARAM, "a_variant must be 0..2, solve_threads 0..256, xy_threads 0, 256 or 512");
+        (xy_threads != 0 && xy_threads != 256 && xy_threads != 512) || xy_half_planes < 0 || xy_half_planes > 1)
+        return set_err(c, WLC_E_PARAM,
+                       "a_variant must be 0..2, solve_threads 0..256, xy_threads 0, 256 or 512, xy_half_planes 0 or 1");
+    c->xy_z = xy_half_planes;
     c->a_variant = a_variant;
     c->solve_threads = solve_threads;
     c->xy_threads = xy_threads;
@@ -1322,7 +1331,7 @@ struct wlc_batch {
         StepArgs<float>* dstep = nullptr;  // [2 directions][nmax + 1][count]
         SolveArgs<float>* dsolve = nullptr;
         size_t smem = 0;
-        int a_variant = 0, solve_threads = 0, xy_threads = 0;
+        int a_variant = 0, solve_threads = 0, xy_threads = 0, xy_z = 0;
     };
     std::vector<Group> groups;
     std::vector<int> streamed;                  // instances with streamed densities
@@ -1482,6 +1491,7 @@ static int batch_issue(wlc_batch* b) {
             bl.a_variant = g.a_variant;
             bl.solve_threads = g.solve_threads;
             bl.xy_threads = g.xy_threads;
+            bl.xy_z = g.xy_z;
             cudaError_t err = launch_step_batched(g.N, bl, b->st);
             b->launches += 3;
             if (err != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("batched step: ") + cudaGetErrorString(err));
@@ -1656,7 +1666,8 @@ extern "C" int wlc_batch_autotune(wlc_batch* b, int32_t* config) {
         auto& g = b->groups[gi];
         const int cnt = (int)g.idx.size();
         float best = 1e30f;
-        int best_a = g.a_variant, best_t = g.solve_threads, best_x = g.xy_threads;
+        int best_a = g.a_variant, best_t = g.solve_threads, best_x = g.xy_threads, best_z = g.xy_z;
+        for (int xz : {0, 1})
         for (int xt : {256, 512})
         for (int av : {1, 2})
             for (int th : solve_thread_candidates(g.N)) {
@@ -1671,6 +1682,7 @@ extern "C" int wlc_batch_autotune(wlc_batch* b, int32_t* config) {
                 bl.a_variant = av;
                 bl.solve_threads = th;
                 bl.xy_threads = xt;
+                bl.xy_z = xz;
                 for (int i : g.idx) {  // Theta terms of that step
                     wlc_ctx* c = b->inst[i];
                     if (!ms_active(c)) continue;
@@ -1688,16 +1700,19 @@ extern "C" int wlc_batch_autotune(wlc_batch* b, int32_t* config) {
                     best_a = av;
                     best_t = th;
                     best_x = xt;
+                    best_z = xz;
                 }
             }
         g.a_variant = best_a;
         g.solve_threads = best_t;
         g.xy_threads = best_x;
+        g.xy_z = best_z;
         if (config) {
-            config[4 * gi] = g.N;
-            config[4 * gi + 1] = best_a;
-            config[4 * gi + 2] = best_t;
-            config[4 * gi + 3] = best_x;
+            config[5 * gi] = g.N;
+            config[5 * gi + 1] = best_a;
+            config[5 * gi + 2] = best_t;
+            config[5 * gi + 3] = best_x;
+            config[5 * gi + 4] = best_z;
         }
     }
     drop_graph(b);

@@ -23,6 +23,13 @@ __host__ __device__ constexpr int zg_planes(int N, int tsize) {
     return z;
 }
 
+// planes per CTA of the generic pass A and pass C in launch variant zd
+// (0: zg_planes; 1: half of it while a plane run stays a whole 16-byte chunk)
+__host__ __device__ constexpr int xy_planes(int N, int tsize, int zd) {
+    const int z = zg_planes(N, tsize);
+    return (zd == 1 && z / 2 >= 1 && ((z / 2) * 2 * tsize) % 16 == 0) ? z / 2 : z;
+}
+
 template <typename T> struct StepArgs {
     using C = typename cvec<T>::t;
     // pass A

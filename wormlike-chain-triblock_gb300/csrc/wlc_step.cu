@@ -102,11 +102,11 @@ __device__ __forceinline__ void store_phat(const StepArgs<T>& a, const typename 
 }
 
 // ---------------------------------------------------------------- pass A
-template <typename T, int N, bool B = false>
+template <typename T, int N, bool B = false, int ZD = 0>
 __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
     const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
-    constexpr int Z = zg_planes(N, sizeof(T));
+    constexpr int Z = xy_planes(N, sizeof(T), ZD);
     constexpr int NR = N * N * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
@@ -208,11 +208,11 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
 }
 
 // ---------------------------------------------------------------- pass C
-template <typename T, int N, bool B = false>
+template <typename T, int N, bool B = false, int ZD = 0>
 __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
     const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
-    constexpr int Z = zg_planes(N, sizeof(T));
+    constexpr int Z = xy_planes(N, sizeof(T), ZD);
     constexpr int NKX = N / 2 + 1;
     constexpr int NR = N * N * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -280,16 +280,18 @@ __global__ void __launch_bounds__(256) rhs_only(StepArgs<T> a, T* out) {
 }
 
 // ------------------------------------------------------------ launchers
-template <typename T> size_t smem_xy(int N) {
+template <typename T> size_t smem_xy(int N, int zd) {
     using C = typename cvec<T>::t;
-    return sizeof(C) * ((size_t)N + (size_t)(N / 2) * N + (size_t)zg_planes(N, sizeof(T)) * N * (N / 2 + 1));
+    return sizeof(C) * ((size_t)N + (size_t)(N / 2) * N + (size_t)xy_planes(N, sizeof(T), zd) * N * (N / 2 + 1));
 }
 
 template <typename T, int N, bool B> static void set_xy_attrs() {
     static bool done = false;
     if (done) return;
-    cudaFuncSetAttribute(rhs_fft_xy<T, N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(ifft_xy<T, N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(ifft_xy<T, N, B, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(ifft_xy<T, N, B, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
         cudaFuncSetAttribute(rhs_fft_xy_staged<N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)StagedA<N>::bytes);
@@ -307,9 +309,30 @@ template <typename T, int N> static bool use_staged(int variant) {
         return false;
 }
 
+// generic pass A / pass C launches in plane variant ZD
+template <typename T, int N, bool B, int ZD>
+static void launch_xy(bool do_a, bool do_c_only, const StepArgs<T>& a, const StepArgs<T>* batch, int M, int count,
+                      int threads, cudaStream_t st) {
+    constexpr int Z = xy_planes(N, sizeof(T), ZD);
+    const size_t sxy = smem_xy<T>(N, ZD);
+    const dim3 g(N / Z, M, count);
+    if (do_a)
+        rhs_fft_xy<T, N, B, ZD><<<g, xy_block(threads), sxy, st>>>(a, batch);
+    else if (do_c_only)
+        ifft_xy<T, N, B, ZD><<<g, xy_block(threads), sxy, st>>>(a, batch);
+}
+
+template <typename T, int N, bool B>
+static void launch_xy_any(int zd, bool do_a, const StepArgs<T>& a, const StepArgs<T>* batch, int M, int count,
+                          int threads, cudaStream_t st) {
+    if (zd == 1)
+        launch_xy<T, N, B, 1>(do_a, !do_a, a, batch, M, count, threads, st);
+    else
+        launch_xy<T, N, B, 0>(do_a, !do_a, a, batch, M, count, threads, st);
+}
+
 template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s, cudaStream_t st) {
     constexpr int Z = zg_planes(N, sizeof(T));
-    const size_t sxy = smem_xy<T>(N);
     set_xy_attrs<T, N, false>();
     const dim3 gxy(N / Z, s.step.M);
     if (s.events) cudaEventRecord(s.events[0], st);
@@ -319,19 +342,18 @@ template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s,
             staged = use_staged<T, N>(s.a_variant);
             if (staged) rhs_fft_xy_staged<N><<<gxy, 512, StagedA<N>::bytes, st>>>(s.step, nullptr);
         }
-        if (!staged) rhs_fft_xy<T, N><<<gxy, xy_block(s.xy_threads), sxy, st>>>(s.step, nullptr);
+        if (!staged) launch_xy_any<T, N, false>(s.xy_z, true, s.step, nullptr, s.step.M, 1, s.xy_threads, st);
     }
     if (s.events) cudaEventRecord(s.events[1], st);
     if (s.do_b) launch_solve<T>(N, s.solve, st, s.solve_threads);
     if (s.events) cudaEventRecord(s.events[2], st);
-    if (s.do_c) ifft_xy<T, N><<<gxy, xy_block(s.xy_threads), sxy, st>>>(s.step, nullptr);
+    if (s.do_c) launch_xy_any<T, N, false>(s.xy_z, false, s.step, nullptr, s.step.M, 1, s.xy_threads, st);
     if (s.events) cudaEventRecord(s.events[3], st);
     return cudaGetLastError();
 }
 
 template <int N> static cudaError_t launch_batched_n(const BatchLaunch<float>& b, cudaStream_t st) {
     constexpr int Z = zg_planes(N, 4);
-    const size_t sxy = smem_xy<float>(N);
     set_xy_attrs<float, N, true>();
     const dim3 gxy(N / Z, b.M, b.count);
     bool staged = false;
@@ -339,10 +361,10 @@ template <int N> static cudaError_t launch_batched_n(const BatchLaunch<float>& b
         staged = use_staged<float, N>(b.a_variant);
         if (staged) rhs_fft_xy_staged<N, true><<<gxy, 512, StagedA<N>::bytes, st>>>(StepArgs<float>{}, b.dstep);
     }
-    if (!staged) rhs_fft_xy<float, N, true><<<gxy, xy_block(b.xy_threads), sxy, st>>>(StepArgs<float>{}, b.dstep);
+    if (!staged) launch_xy_any<float, N, true>(b.xy_z, true, StepArgs<float>{}, b.dstep, b.M, b.count, b.xy_threads, st);
     cudaError_t e = launch_solve_batched(N, b, st);
     if (e != cudaSuccess) return e;
-    ifft_xy<float, N, true><<<gxy, xy_block(b.xy_threads), sxy, st>>>(StepArgs<float>{}, b.dstep);
+    launch_xy_any<float, N, true>(b.xy_z, false, StepArgs<float>{}, b.dstep, b.M, b.count, b.xy_threads, st);
     return cudaGetLastError();
 }
 
@@ -404,7 +426,7 @@ template cudaError_t launch_rhs_only<double>(int, const StepArgs<double>&, doubl
 template cudaError_t launch_rhs_only<float>(int, const StepArgs<float>&, float*, cudaStream_t);
 template cudaError_t launch_step<double>(int, const StepLaunch<double>&, cudaStream_t);
 template cudaError_t launch_step<float>(int, const StepLaunch<float>&, cudaStream_t);
-template size_t smem_xy<double>(int);
-template size_t smem_xy<float>(int);
+template size_t smem_xy<double>(int, int);
+template size_t smem_xy<float>(int, int);
 
 }  // namespace wlc

@@ -18,6 +18,7 @@ template <typename T> struct StepLaunch {
     int a_variant = 0;      // pass A: 0 default, 1 generic, 2 staged (FP32, where it fits)
     int solve_threads = 0;  // pass B threads per CTA (0: default)
     int xy_threads = 0;     // generic pass A and pass C threads per CTA (256 or 512; 0: 256)
+    int xy_z = 0;           // generic pass A and pass C planes per CTA: 0 default, 1 half
     cudaEvent_t* events = nullptr;  // 4 events around the three passes, or null
 };
 
@@ -28,12 +29,12 @@ template <typename T> struct BatchLaunch {
     const SolveArgs<T>* dsolve = nullptr;
     int count = 0, M = 0, nkx = 0;
     size_t solve_smem = 0;
-    int a_variant = 0, solve_threads = 0, xy_threads = 0;
+    int a_variant = 0, solve_threads = 0, xy_threads = 0, xy_z = 0;
 };
 
 template <typename T> cudaError_t launch_step(int N, const StepLaunch<T>& s, cudaStream_t st);
 template <typename T> cudaError_t launch_rhs_only(int N, const StepArgs<T>& a, T* out, cudaStream_t st);
-template <typename T> size_t smem_xy(int N);
+template <typename T> size_t smem_xy(int N, int zd = 0);
 template <typename T> cudaError_t launch_solve(int N, const SolveArgs<T>& a, cudaStream_t st, int threads = 0);
 cudaError_t launch_step_batched(int N, const BatchLaunch<float>& b, cudaStream_t st);
 cudaError_t launch_solve_batched(int N, const BatchLaunch<float>& b, cudaStream_t st);

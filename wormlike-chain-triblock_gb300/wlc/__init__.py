@@ -144,7 +144,7 @@ def load(build_if_missing=True):
     lib.wlc_net_train.argtypes = [P, Fp, Fp, I, I, I, ctypes.c_float, ctypes.c_uint64, Dp]
     Ip = ctypes.POINTER(ctypes.c_int32)
     lib.wlc_autotune.argtypes = [P, Ip]
-    lib.wlc_set_launch_config.argtypes = [P, I, I, I]
+    lib.wlc_set_launch_config.argtypes = [P, I, I, I, I]
     lib.wlc_batch_create.argtypes = [ctypes.POINTER(Params), I, ctypes.POINTER(P)]
     lib.wlc_batch_destroy.argtypes = [P]
     lib.wlc_batch_last_error.argtypes = [P]
@@ -374,13 +374,14 @@ class Instance:
     def autotune(self):
         """Time the launch configurations of a contour step on this
         instance's data and keep the fastest; returns (a_variant,
-        solve_threads, xy_threads)."""
-        cfg = (ctypes.c_int32 * 3)()
+        solve_threads, xy_threads, xy_half_planes)."""
+        cfg = (ctypes.c_int32 * 4)()
         self._check(self.lib.wlc_autotune(self.h, cfg))
-        return int(cfg[0]), int(cfg[1]), int(cfg[2])
+        return tuple(int(v) for v in cfg)
 
-    def set_launch_config(self, a_variant=0, solve_threads=0, xy_threads=0):
-        self._check(self.lib.wlc_set_launch_config(self.h, int(a_variant), int(solve_threads), int(xy_threads)))
+    def set_launch_config(self, a_variant=0, solve_threads=0, xy_threads=0, xy_half_planes=0):
+        self._check(self.lib.wlc_set_launch_config(self.h, int(a_variant), int(solve_threads), int(xy_threads),
+                                                   int(xy_half_planes)))
 
     def reset_mixing(self):
         self._check(self.lib.wlc_reset_mixing(self.h))
@@ -473,9 +474,9 @@ class Batch:
 
     def autotune(self):
         g = self.lib.wlc_batch_groups(self.h)
-        cfg = (ctypes.c_int32 * (4 * max(1, g)))()
+        cfg = (ctypes.c_int32 * (5 * max(1, g)))()
         self._check(self.lib.wlc_batch_autotune(self.h, cfg))
-        return [tuple(int(cfg[4 * i + k]) for k in range(4)) for i in range(g)]
+        return [tuple(int(cfg[5 * i + k]) for k in range(5)) for i in range(g)]
 
     def use_graph(self, on=True):
         self._check(self.lib.wlc_batch_use_graph(self.h, 1 if on else 0))
