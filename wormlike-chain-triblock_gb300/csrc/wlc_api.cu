@@ -1332,11 +1332,15 @@ struct wlc_batch {
         SolveArgs<float>* dsolve = nullptr;
         size_t smem = 0;
         int a_variant = 0, solve_threads = 0, xy_threads = 0, xy_z = 0;
+        std::vector<int> streamed;              // members with streamed densities
+        SliceBatchArgs<float>* dslice = nullptr;  // [streamed]
+        bool any_s = false;
+        cudaStream_t st = nullptr;  // the group's stream inside the captured contour loop
+        cudaEvent_t done = nullptr;
     };
+    cudaEvent_t fork = nullptr;
     std::vector<Group> groups;
-    std::vector<int> streamed;                  // instances with streamed densities
-    SliceBatchArgs<float>* dslice = nullptr;    // [streamed]
-    int64_t max_nr_streamed = 0;
+    std::vector<int> streamed;  // instances with streamed densities
     std::vector<void*> allocs;
     std::vector<long> sig;  // per instance: box generation and Maier-Saupe state at the last build
     bool built = false;
@@ -1437,9 +1441,11 @@ static int batch_build(wlc_batch* b) {
         BCK(cudaMemcpy(g.dstep, hs.data(), sizeof(StepArgs<float>) * tot, cudaMemcpyHostToDevice));
         BCK(cudaMemcpy(g.dsolve, hv.data(), sizeof(SolveArgs<float>) * tot, cudaMemcpyHostToDevice));
     }
-    if (!b->streamed.empty()) {
+    for (auto& g : b->groups) {
+        if (g.streamed.empty()) continue;
         std::vector<SliceBatchArgs<float>> ha;
-        for (int i : b->streamed) {
+        g.any_s = false;
+        for (int i : g.streamed) {
             wlc_ctx* c = b->inst[i];
             SliceBatchArgs<float> a;
             a.qf = (const float*)c->qf;
@@ -1452,83 +1458,100 @@ static int batch_build(wlc_batch* b) {
             a.junc = c->junc;
             a.qend = c->qend;
             a.sraw = c->sraw;
+            g.any_s = g.any_s || a.want_s;
             ha.push_back(a);
         }
         int rc;
-        if (!b->dslice && (rc = balloc(b, &b->dslice, sizeof(SliceBatchArgs<float>) * ha.size()))) return rc;
-        BCK(cudaMemcpy(b->dslice, ha.data(), sizeof(SliceBatchArgs<float>) * ha.size(), cudaMemcpyHostToDevice));
+        if (!g.dslice && (rc = balloc(b, &g.dslice, sizeof(SliceBatchArgs<float>) * ha.size()))) return rc;
+        BCK(cudaMemcpy(g.dslice, ha.data(), sizeof(SliceBatchArgs<float>) * ha.size(), cudaMemcpyHostToDevice));
     }
     b->sig = batch_signature(b);
     b->built = true;
     return WLC_OK;
 }
 
-// enqueue the forward and backward sweeps of every instance on the batch stream
-static int batch_issue(wlc_batch* b) {
+// enqueue the forward and backward sweeps of one grid-size group on stream st
+static int batch_issue_group(wlc_batch* b, wlc_batch::Group& g, cudaStream_t st) {
     const int nmax = b->nmax;
-    auto step_all = [&](int d, int n) -> int {
+    const int cnt = (int)g.idx.size();
+    auto step = [&](int d, int n) -> int {
         const int dir = d == 0 ? 1 : -1;
-        for (auto* c : b->inst) {
+        for (int i : g.idx) {
+            wlc_ctx* c = b->inst[i];
             if (!ms_active(c)) continue;
             const float* h[3];
             float* out;
             StepKind k;
             step_ptrs(c, dir, n, h, &out, &k);
             launch_ms_term<float>(h[0], h[1], h[2], k.order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M,
-                                  c->nr, (float*)c->msterm, b->st);
+                                  c->nr, (float*)c->msterm, st);
             b->launches++;
         }
-        for (auto& g : b->groups) {
-            BatchLaunch<float> bl;
-            const int cnt = (int)g.idx.size();
-            const size_t e = ((size_t)d * (nmax + 1) + n) * cnt;
-            bl.dstep = g.dstep + e;
-            bl.dsolve = g.dsolve + e;
-            bl.count = cnt;
-            bl.M = b->M;
-            bl.nkx = g.N / 2 + 1;
-            bl.solve_smem = g.smem;
-            bl.a_variant = g.a_variant;
-            bl.solve_threads = g.solve_threads;
-            bl.xy_threads = g.xy_threads;
-            bl.xy_z = g.xy_z;
-            cudaError_t err = launch_step_batched(g.N, bl, b->st);
-            b->launches += 3;
-            if (err != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("batched step: ") + cudaGetErrorString(err));
-        }
+        BatchLaunch<float> bl;
+        const size_t e = ((size_t)d * (nmax + 1) + n) * cnt;
+        bl.dstep = g.dstep + e;
+        bl.dsolve = g.dsolve + e;
+        bl.count = cnt;
+        bl.M = b->M;
+        bl.nkx = g.N / 2 + 1;
+        bl.solve_smem = g.smem;
+        bl.a_variant = g.a_variant;
+        bl.solve_threads = g.solve_threads;
+        bl.xy_threads = g.xy_threads;
+        bl.xy_z = g.xy_z;
+        cudaError_t err = launch_step_batched(g.N, bl, st);
+        b->launches += 3;
+        if (err != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("batched step: ") + cudaGetErrorString(err));
         return WLC_OK;
     };
     auto slices = [&](int s) {
-        if (b->streamed.empty()) return;
-        bool any_s = false;
-        for (int i : b->streamed) any_s = any_s || stream_s(b->inst[i]);
-        launch_density_slice_batched<float>(b->dslice, (int)b->streamed.size(), b->max_nr_streamed, s, b->M,
-                                            b->inst[b->streamed[0]]->jl.n, any_s ? 1 : 0, b->st);
+        if (g.streamed.empty()) return;
+        const wlc_ctx* c0 = b->inst[g.streamed[0]];
+        launch_density_slice_batched<float>(g.dslice, (int)g.streamed.size(), c0->nr, s, b->M, c0->jl.n,
+                                            g.any_s ? 1 : 0, st);
         b->launches++;
     };
     int rc;
-    for (auto* c : b->inst) {
-        launch_set_delta<float>((float*)c->qf, c->M, c->nr, b->st);
+    for (int i : g.idx) {
+        wlc_ctx* c = b->inst[i];
+        launch_set_delta<float>((float*)c->qf, c->M, c->nr, st);
         b->launches++;
     }
     for (int n = 1; n <= nmax; ++n)
-        if ((rc = step_all(0, n))) return rc;
-    for (int i : b->streamed) {
+        if ((rc = step(0, n))) return rc;
+    for (int i : g.streamed) {
         wlc_ctx* c = b->inst[i];
-        BCK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, b->st));
-        if (stream_s(c)) BCK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, b->st));
+        BCK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, st));
+        if (stream_s(c)) BCK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, st));
     }
-    for (auto* c : b->inst) {
-        launch_set_delta<float>(qb_at<float>(c, nmax), c->M, c->nr, b->st);
+    for (int i : g.idx) {
+        wlc_ctx* c = b->inst[i];
+        launch_set_delta<float>(qb_at<float>(c, nmax), c->M, c->nr, st);
         b->launches++;
     }
     slices(nmax);
     for (int n = 1; n <= nmax; ++n) {
-        if ((rc = step_all(1, n))) return rc;
+        if ((rc = step(1, n))) return rc;
         slices(nmax - n);
     }
     BCK(cudaGetLastError());
     return WLC_OK;
+}
+
+// enqueue the sweeps of every instance: the groups are independent, so each
+// runs on its own stream (forked from and joined back into the batch
+// stream; inside stream capture this becomes parallel branches of the graph)
+static int batch_issue(wlc_batch* b) {
+    if (b->groups.size() == 1) return batch_issue_group(b, b->groups[0], b->st);
+    BCK(cudaEventRecord(b->fork, b->st));
+    int rc = WLC_OK;
+    for (auto& g : b->groups) {
+        BCK(cudaStreamWaitEvent(g.st, b->fork, 0));
+        if ((rc = batch_issue_group(b, g, g.st))) break;
+        BCK(cudaEventRecord(g.done, g.st));
+    }
+    for (auto& g : b->groups) BCK(cudaStreamWaitEvent(b->st, g.done, 0));
+    return rc;
 }
 
 extern "C" int wlc_batch_create(const wlc_params* p, int32_t count, wlc_batch** out) {
@@ -1574,10 +1597,16 @@ extern "C" int wlc_batch_create(const wlc_params* p, int32_t count, wlc_batch** 
         }
         if (c->stream) {
             b->streamed.push_back(i);
-            b->max_nr_streamed = std::max<int64_t>(b->max_nr_streamed, c->nr);
+            for (auto& g : b->groups)
+                if (g.N == c->N) g.streamed.push_back(i);
         }
     }
-    for (auto& g : b->groups) BCK(prepare_step_batched(g.N));
+    for (auto& g : b->groups) {
+        BCK(prepare_step_batched(g.N));
+        BCK(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
+        BCK(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
+    }
+    BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     return WLC_OK;
 }
 
@@ -1587,6 +1616,14 @@ extern "C" int wlc_batch_destroy(wlc_batch* b) {
     drop_graph(b);
     for (auto* c : b->inst) destroy_impl(c);
     for (void* q : b->allocs) cudaFree(q);
+    for (auto& g : b->groups) {
+        if (g.st) {
+            cudaStreamSynchronize(g.st);
+            cudaStreamDestroy(g.st);
+        }
+        if (g.done) cudaEventDestroy(g.done);
+    }
+    if (b->fork) cudaEventDestroy(b->fork);
     if (b->st) cudaStreamDestroy(b->st);
     delete b;
     return WLC_OK;
