@@ -56,6 +56,27 @@ __device__ __forceinline__ T rhs_value(const StepArgs<T>& a, size_t off, size_t 
     return v;
 }
 
+// rhs_value for four consecutive points (FP32; off and r multiples of 4)
+__device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
+__device__ __forceinline__ float4 rhs_f32x4(const StepArgs<float>& a, size_t off, size_t r) {
+    const int o = a.order;
+    const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 q1 = ld4(a.h1 + off);
+    const float4 q2 = o >= 2 ? ld4(a.h2 + off) : z4;
+    const float4 q3 = o >= 3 ? ld4(a.h3 + off) : z4;
+    const float4 dw = o >= 1 ? ld4(a.dsw + r) : z4;
+    float4 v = make_float4(rhs_f32(o, q1.x, q2.x, q3.x, dw.x, a.third), rhs_f32(o, q1.y, q2.y, q3.y, dw.y, a.third),
+                           rhs_f32(o, q1.z, q2.z, q3.z, dw.z, a.third), rhs_f32(o, q1.w, q2.w, q3.w, dw.w, a.third));
+    if (a.msterm) {
+        const float4 m = ld4(a.msterm + off);
+        v.x += m.x;
+        v.y += m.y;
+        v.z += m.z;
+        v.w += m.w;
+    }
+    return v;
+}
+
 // ------------------------------------------------------- async copies
 __device__ __forceinline__ void cp_async16(void* sdst, const void* gsrc) {
     const unsigned sa = (unsigned)__cvta_generic_to_shared(sdst);
@@ -117,12 +138,28 @@ __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
     for (int zz = 0; zz < Z; ++zz) {
         const int z = z0 + zz;
-        for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
-            const int p = e / N, x = e % N;
-            const size_t ra = ((size_t)z * N + 2 * p) * N + x, rb = ra + N;
-            const T va = rhs_value<T, NR>(a, (size_t)i * NR + ra, ra);
-            const T vb = rhs_value<T, NR>(a, (size_t)i * NR + rb, rb);
-            zb[e] = cmk<C>(va, vb);
+        if constexpr (sizeof(T) == 4) {
+            // four consecutive x per thread: 16-byte loads of the history, ds*w
+            // and Theta planes (N is a multiple of 4)
+            for (int e4 = threadIdx.x; e4 < (N / 2) * N / 4; e4 += blockDim.x) {
+                const int e = 4 * e4;
+                const int p = e / N, x = e % N;
+                const size_t ra = ((size_t)z * N + 2 * p) * N + x, rb = ra + N;
+                const float4 va = rhs_f32x4(a, (size_t)i * NR + ra, ra);
+                const float4 vb = rhs_f32x4(a, (size_t)i * NR + rb, rb);
+                zb[e] = cmk<C>(va.x, vb.x);
+                zb[e + 1] = cmk<C>(va.y, vb.y);
+                zb[e + 2] = cmk<C>(va.z, vb.z);
+                zb[e + 3] = cmk<C>(va.w, vb.w);
+            }
+        } else {
+            for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
+                const int p = e / N, x = e % N;
+                const size_t ra = ((size_t)z * N + 2 * p) * N + x, rb = ra + N;
+                const T va = rhs_value<T, NR>(a, (size_t)i * NR + ra, ra);
+                const T vb = rhs_value<T, NR>(a, (size_t)i * NR + rb, rb);
+                zb[e] = cmk<C>(va, vb);
+            }
         }
         __syncthreads();
         fwd_xy_plane<T, N, Z>(zb, out, zz, tw);
