@@ -90,10 +90,11 @@ template <int n> __device__ __forceinline__ void cp_async_wait() {
 // The half-spectrum planes of a CTA are kept z-fastest, out[(ky*NKX + kx)*Z + zz],
 // so that the Z values of one (col, i) run in phat move as one 32-byte chunk.
 
-// x-FFT of packed row pairs, split into two half spectra, y-FFT; plane zz of out
+// x-FFT of packed row pairs, split into two half spectra; plane zz of out
+// (the y-FFTs of all planes follow in one batched call, fwd_y_planes)
 template <typename T, int N, int Z>
-__device__ __forceinline__ void fwd_xy_plane(typename cvec<T>::t* zb, typename cvec<T>::t* out, int zz,
-                                             const typename cvec<T>::t* tw) {
+__device__ __forceinline__ void fwd_x_plane(typename cvec<T>::t* zb, typename cvec<T>::t* out, int zz,
+                                            const typename cvec<T>::t* tw) {
     using C = typename cvec<T>::t;
     constexpr int NKX = N / 2 + 1;
     fft_nat2perm<N, -1>(zb, N / 2, 1, N, tw);
@@ -105,7 +106,14 @@ __device__ __forceinline__ void fwd_xy_plane(typename cvec<T>::t* zb, typename c
         out[((2 * p + 1) * NKX + k) * Z + zz] = cmk<C>((T)0.5 * (zk.y + zm.y), (T)0.5 * (zm.x - zk.x));
     }
     __syncthreads();
-    fft_nat2perm<N, -1>(out + zz, NKX, NKX * Z, Z, tw);
+}
+
+// y-FFTs of every (kx, plane) line of out: line kx*Z + zz starts at out + kx*Z + zz,
+// element ky at stride NKX*Z
+template <typename T, int N, int Z, int DIR>
+__device__ __forceinline__ void y_planes(typename cvec<T>::t* out, const typename cvec<T>::t* tw) {
+    constexpr int NKX = N / 2 + 1;
+    fft_nat2perm<N, DIR>(out, NKX * Z, NKX * Z, 1, tw);
 }
 
 template <typename T, int N, int Z>
@@ -162,8 +170,9 @@ __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs
             }
         }
         __syncthreads();
-        fwd_xy_plane<T, N, Z>(zb, out, zz, tw);
+        fwd_x_plane<T, N, Z>(zb, out, zz, tw);
     }
+    y_planes<T, N, Z, -1>(out, tw);
     store_phat<T, N, Z>(a, out, i, z0);
 }
 
@@ -239,8 +248,9 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
             zb[e] = make_float2(va, vb);
         }
         __syncthreads();
-        fwd_xy_plane<float, N, Z>(zb, out, zz, tw);
+        fwd_x_plane<float, N, Z>(zb, out, zz, tw);
     }
+    y_planes<float, N, Z, -1>(out, tw);
     store_phat<float, N, Z>(a, out, i, z0);
 }
 
@@ -271,8 +281,8 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
     cp_async_commit();
     cp_async_wait<0>();
     __syncthreads();
+    y_planes<T, N, Z, +1>(out, tw);  // along y for every plane; row y now at perm_pos(y)
     for (int zz = 0; zz < Z; ++zz) {
-        fft_nat2perm<N, +1>(out + zz, NKX, NKX * Z, Z, tw);  // along y; row y now at perm_pos(y)
         // Hermitian extension of rows (2p, 2p+1) packed as one complex row;
         // the imaginary parts at kx = 0 and N/2 are discarded (c2r)
         for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
