@@ -77,7 +77,37 @@ __global__ void make_cf(const double* __restrict__ w, T* __restrict__ cf, double
 // Maier-Saupe term ds * sum_j Theta_ij(r) h_j(r), h the BDF history
 // combination of the given order (calc_THETAij and the Theta loop of
 // init_pr, wormlike_MDE_2dcomp_mod.f90:5-110, MDE_ABC.f90:256-268).
-// shared-memory layout of ms_term: val[5n] | hc[M][TILE] | rowptr[M+1] | col[n]
+// 16-byte vector access of 16/sizeof(T) consecutive values (16-byte aligned)
+template <typename T> struct VecOf;
+template <> struct VecOf<float> { using t = float4; };
+template <> struct VecOf<double> { using t = double2; };
+template <typename T> __device__ __forceinline__ void vload(const T* p, T* v) {
+    const typename VecOf<T>::t x = *reinterpret_cast<const typename VecOf<T>::t*>(p);
+    if constexpr (sizeof(T) == 4) {
+        v[0] = x.x;
+        v[1] = x.y;
+        v[2] = x.z;
+        v[3] = x.w;
+    } else {
+        v[0] = x.x;
+        v[1] = x.y;
+    }
+}
+template <typename T> __device__ __forceinline__ void vstore(T* p, const T* v) {
+    typename VecOf<T>::t x;
+    if constexpr (sizeof(T) == 4) {
+        x.x = v[0];
+        x.y = v[1];
+        x.z = v[2];
+        x.w = v[3];
+    } else {
+        x.x = v[0];
+        x.y = v[1];
+    }
+    *reinterpret_cast<typename VecOf<T>::t*>(p) = x;
+}
+
+// shared-memory layout of ms_term: hc[M][TILE] (16-byte aligned rows) | val[5n] | rowptr[M+1] | col[n]
 template <typename T> __host__ __device__ inline size_t ms_smem_bytes(int n, int M) {
     return sizeof(T) * ((size_t)5 * n + (size_t)M * PointTile<T>::value) + sizeof(int) * (size_t)(M + 1) +
            sizeof(int16_t) * (size_t)n;
@@ -93,9 +123,9 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
             T* __restrict__ out) {
     constexpr int TILE = PointTile<T>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    T* sval = reinterpret_cast<T*>(smem_raw);
-    T* hc = sval + (size_t)5 * tl.n;  // [M][TILE]: BDF history combination of the tile's points
-    int* srp = reinterpret_cast<int*>(hc + (size_t)M * TILE);
+    T* hc = reinterpret_cast<T*>(smem_raw);  // [M][TILE]: BDF history combination of the tile's points
+    T* sval = hc + (size_t)M * TILE;
+    int* srp = reinterpret_cast<int*>(sval + (size_t)5 * tl.n);
     int16_t* scol = reinterpret_cast<int16_t*>(srp + M + 1);
     for (int e = threadIdx.x; e < 5 * tl.n; e += blockDim.x) sval[e] = (T)tl.val[e];
     for (int e = threadIdx.x; e <= M; e += blockDim.x) srp[e] = tl.rowptr[e];
@@ -104,21 +134,32 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
     const T th_min = (T)thresh;
     for (int64_t r0 = (int64_t)blockIdx.x * TILE; r0 < nr; r0 += (int64_t)gridDim.x * TILE) {
         __syncthreads();  // tables staged / previous tile consumed
-        for (int idx = threadIdx.x; idx < M * TILE; idx += blockDim.x) {
-            const int j = idx / TILE, kk = idx % TILE;
+        // 16-byte vectors of V consecutive points (nr and r0 are multiples of V)
+        constexpr int V = 16 / sizeof(T);
+        using VT = typename VecOf<T>::t;
+        for (int idx = threadIdx.x; idx < M * (TILE / V); idx += blockDim.x) {
+            const int j = idx / (TILE / V), kk = (idx % (TILE / V)) * V;
             const int64_t r = r0 + kk;
-            T v = (T)0;
+            T v[V] = {};
             if (r < nr) {
                 const int64_t o = (int64_t)j * nr + r;
-                if (order == 1)
-                    v = h1[o];
-                else if (order == 2)
-                    v = (T)2 * h1[o] - h2[o];
-                else
-                    v = (T)3 * h1[o] - (T)3 * h2[o] + h3[o];
+                T q1[V], q2[V], q3[V];
+                vload<T>(h1 + o, q1);
+                if (order >= 2) vload<T>(h2 + o, q2);
+                if (order >= 3) vload<T>(h3 + o, q3);
+#pragma unroll
+                for (int u = 0; u < V; ++u) {
+                    if (order == 1)
+                        v[u] = q1[u];
+                    else if (order == 2)
+                        v[u] = (T)2 * q1[u] - q2[u];
+                    else
+                        v[u] = (T)3 * q1[u] - (T)3 * q2[u] + q3[u];
+                }
             }
-            hc[idx] = v;
+            vstore<T>(hc + j * TILE + kk, v);
         }
+        (void)sizeof(VT);
         __syncthreads();
         const int64_t r = r0 + k;
         if (r >= nr) continue;
@@ -127,15 +168,25 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
         const T coef[5] = {(T)(mop[0 * nr + r] - mop[4 * nr + r]), (T)mop[8 * nr + r], (T)mop[3 * nr + r],
                            (T)mop[6 * nr + r], (T)mop[7 * nr + r]};
         const T* hv = hc + k;
+        // entries in groups of four with independent partial sums (the list
+        // loads and the coefficient gathers of four entries overlap)
+        auto term = [&](int e) -> T {
+            const T* v5 = sval + 5 * e;
+            const T th = coef[0] * v5[0] + coef[1] * v5[1] + coef[2] * v5[2] + coef[3] * v5[3] + coef[4] * v5[4];
+            return fabs(th) < th_min ? (T)0 : th * hv[scol[e] * TILE];
+        };
         for (int i = g; i < M; i += kMsGroups) {
-            T acc = (T)0;
-            for (int e = srp[i]; e < srp[i + 1]; ++e) {
-                const T* v5 = sval + 5 * e;
-                const T th = coef[0] * v5[0] + coef[1] * v5[1] + coef[2] * v5[2] + coef[3] * v5[3] + coef[4] * v5[4];
-                if (fabs(th) < th_min) continue;
-                acc += th * hv[scol[e] * TILE];
+            T a0 = (T)0, a1 = (T)0, a2 = (T)0, a3 = (T)0;
+            const int e1 = srp[i + 1];
+            int e = srp[i];
+            for (; e + 4 <= e1; e += 4) {
+                a0 += term(e);
+                a1 += term(e + 1);
+                a2 += term(e + 2);
+                a3 += term(e + 3);
             }
-            out[(int64_t)i * nr + r] = (T)ds * acc;
+            for (; e < e1; ++e) a0 += term(e);
+            out[(int64_t)i * nr + r] = (T)ds * ((a0 + a1) + (a2 + a3));
         }
     }
 }
@@ -226,17 +277,22 @@ template <typename T> __device__ __forceinline__ void stage_jlists(const JLists&
 }
 
 // stage the coefficient vectors of one slice for the tile's points (zeros
-// past the end of the grid)
+// past the end of the grid), 16-byte vectors of consecutive points
 template <typename T>
 __device__ __forceinline__ void stage_tile(const T* __restrict__ a, const T* __restrict__ c, int M, int64_t nr,
                                            int64_t r0, T* sa, T* sc) {
     constexpr int TILE = PointTile<T>::value;
-    for (int idx = threadIdx.x; idx < M * TILE; idx += blockDim.x) {
-        const int i = idx / TILE, k = idx % TILE;
+    constexpr int V = 16 / sizeof(T);
+    for (int idx = threadIdx.x; idx < M * (TILE / V); idx += blockDim.x) {
+        const int i = idx / (TILE / V), k = (idx % (TILE / V)) * V;
         const int64_t r = r0 + k;
-        const bool ok = r < nr;
-        sa[idx] = ok ? a[(int64_t)i * nr + r] : (T)0;
-        sc[idx] = ok ? c[(int64_t)i * nr + r] : (T)0;
+        T va[V] = {}, vc[V] = {};
+        if (r < nr) {
+            vload<T>(a + (int64_t)i * nr + r, va);
+            vload<T>(c + (int64_t)i * nr + r, vc);
+        }
+        vstore<T>(sa + i * TILE + k, va);
+        vstore<T>(sc + i * TILE + k, vc);
     }
 }
 
