@@ -2,127 +2,8 @@
 // owning its CUDA stream and device memory.  Sweep drivers follow
 // ABC_melt_driver (MDE_ABC.f90:8-88); density / free energy follow
 // SCFT_Density_FE_ABC.f90:3-271 and SCFT_Density_FE.f90:273-342.
-#include <algorithm>
-#include <cmath>
-#include <cstdio>
-#include <cstring>
-#include <string>
-#include <vector>
-
-#include "wlc.h"
-#include "wlc_internal.h"
-#include "wlc_mix.h"
+#include "wlc_ctx.h"
 #include "wlc_rot_gen.cuh"
-#include "wlc_reduce.h"
-#include "wlc_step.h"
-
-using namespace wlc;
-
-struct wlc_ctx {
-    wlc_params p{};
-    int N = 0, L = 0, M = 0, nkx = 0;
-    int64_t nr = 0, nk = 0;
-    bool fp32 = false;
-    int real4 = 1;
-    double ds = 0, vol = 0, kf[3] = {0, 0, 0};
-    int nstart[3] = {0, 0, 0};
-    void* pivtab = nullptr;  // [order 1..3][blk][key][npiv] compute type, isotropic spacing only
-    int nkeys = 0, npiv = 0;
-    bool have_piv = false;
-    cudaStream_t st = nullptr;
-    std::string err;
-    BasisTables tab;
-    std::vector<void*> allocs;
-    SolveTablesT<double> sd{};
-    SolveTablesT<float> sf{};
-    ThetaLists thl{};
-    JLists jl{};
-    void* twg = nullptr;
-    // per-precision operator data ([0] FP64, [1] FP32); twg / pivtab /
-    // have_piv above alias the active one
-    struct PrecState {
-        bool built = false;
-        void* twg = nullptr;
-        void* pivtab = nullptr;
-        bool have_piv = false;
-        int piv_gen = -1;
-    } prec[2];
-    int box_gen = 0;   // incremented by every wlc_set_box
-    size_t elem = 0;   // bytes per real of the propagator buffers as allocated
-    // propagator storage: qf holds all Nmax+1 slices of q, or (q_checkpoint K
-    // > 0) a 4-slice ring, the BDF3 history triple at every K-th slice and a
-    // (K+2)-slice segment buffer; qb holds all slices of q* or (streamed
-    // densities) a 4-slice ring
-    void* qf = nullptr;
-    void* qb = nullptr;
-    int K = 0, nck = 0;
-    bool stream = false;
-    bool own_stream = true;   // false: the stream belongs to a batch
-    bool batch_owned = false;
-    int a_variant = 0, solve_threads = 0, xy_threads = 0, xy_z = 0;  // launch configuration (autotuned or default)
-    void* phat = nullptr;
-    void* cf = nullptr;
-    void* work = nullptr;    // [M][nr] compute type: RHS / one-step scratch
-    void* msterm = nullptr;  // [M][nr] compute type: Maier-Saupe term
-    double* w = nullptr;
-    double* mop = nullptr;
-    double* raw = nullptr;   // [3][nr]
-    double* junc = nullptr;  // [3][nr] (unscaled)
-    double* juncs = nullptr; // [3][nr] scaled copy
-    double* qend = nullptr;  // [nr]
-    double* phi = nullptr;   // [3][nr]
-    double* part = nullptr;  // [kS3Blocks]
-    double* scal = nullptr;  // [8]
-    double* sraw = nullptr;  // [3][5][nr] (unscaled)
-    double* srs = nullptr;   // [3][5][nr] scaled copy
-    double* ar = nullptr;    // [nr]
-    double* stage = nullptr; // [M*nr] double, host transfer staging
-    int* flag = nullptr;
-    bool have_fields = false, have_mop = false, have_fwd = false, have_bwd = false, have_density = false;
-    double lnq = 0.0, totden = 0.0;
-    int64_t launches = 0;
-    bool timing = false;
-    std::vector<cudaEvent_t> ev;
-    double tms[4] = {0, 0, 0, 0};
-    // field update (wlc_iterate)
-    int mix_iter = 0, mix_depth = -1;
-    double* wout_hist = nullptr;  // [depth+1][3][nr]
-    double* dw_hist = nullptr;    // [depth+1][3][nr]
-    double* mixbuf = nullptr;     // partials / results / coefficients
-};
-
-static int set_err(wlc_ctx* c, int code, const std::string& msg) {
-    if (c) c->err = msg;
-    return code;
-}
-
-#define CK(call)                                                                                          \
-    do {                                                                                                  \
-        cudaError_t e_ = (call);                                                                          \
-        if (e_ != cudaSuccess)                                                                            \
-            return set_err(c, WLC_E_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));            \
-    } while (0)
-
-template <typename X> static int dalloc(wlc_ctx* c, X** ptr, size_t bytes) {
-    void* p = nullptr;
-    cudaError_t e = cudaMalloc(&p, bytes ? bytes : 16);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        char buf[200];
-        std::snprintf(buf, sizeof buf, "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
-        return set_err(c, WLC_E_ALLOC, buf);
-    }
-    c->allocs.push_back(p);
-    *ptr = reinterpret_cast<X*>(p);
-    return WLC_OK;
-}
-
-template <typename X> static int upload(wlc_ctx* c, X** dst, const std::vector<X>& v) {
-    int rc = dalloc(c, dst, sizeof(X) * v.size());
-    if (rc) return rc;
-    if (!v.empty()) CK(cudaMemcpy((void*)*dst, v.data(), sizeof(X) * v.size(), cudaMemcpyHostToDevice));
-    return WLC_OK;
-}
 
 template <typename T> static int build_solve_tables(wlc_ctx* c, SolveTablesT<T>& s) {
     const BasisTables& t = c->tab;
@@ -402,7 +283,7 @@ template <typename T> static int use_precision(wlc_ctx* c) {
     return WLC_OK;
 }
 
-static int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
+int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
     if (!p || !out) return WLC_E_PARAM;
     *out = nullptr;
     wlc_ctx* c = new wlc_ctx();
@@ -520,15 +401,13 @@ static int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
 
 extern "C" int wlc_create(const wlc_params* p, wlc_ctx** out) { return create_impl(p, nullptr, out); }
 
-static int destroy_impl(wlc_ctx* c);
-
 extern "C" int wlc_destroy(wlc_ctx* c) {
     if (!c) return WLC_OK;
     if (c->batch_owned) return set_err(c, WLC_E_STATE, "this context belongs to a batch (wlc_batch_destroy)");
     return destroy_impl(c);
 }
 
-static int destroy_impl(wlc_ctx* c) {
+int destroy_impl(wlc_ctx* c) {
     if (!c) return WLC_OK;
     if (c->st) cudaStreamSynchronize(c->st);
     for (void* p : c->allocs) cudaFree(p);
@@ -537,8 +416,6 @@ static int destroy_impl(wlc_ctx* c) {
     delete c;
     return WLC_OK;
 }
-
-static bool ready(wlc_ctx* c) { return c && c->st; }
 
 extern "C" int wlc_set_box(wlc_ctx* c, double dx, double dy, double dz) {
     if (!ready(c)) return WLC_E_STATE;
@@ -591,75 +468,6 @@ extern "C" int wlc_set_fields(wlc_ctx* c, const double* w, const double* m_op) {
     return WLC_OK;
 }
 
-// (order, sigma, block) of one contour step
-struct StepKind {
-    int order, sigma, blk;
-};
-
-// Maier-Saupe coupling switched on (|NMu| >= 1e-5, as the reference tests it)
-static bool ms_on(const wlc_ctx* c) { return std::fabs(c->p.nmu) >= 1.0e-5; }
-// orientation tensor accumulated by a streamed backward sweep
-static bool stream_s(const wlc_ctx* c) { return c->p.store_qstar == 2 || ms_on(c); }
-
-static int blk_fwd(const wlc_ctx* c, int s) {  // MDE_ABC.f90:44-57
-    if (s <= c->nstart[1]) return 0;
-    if (s <= c->nstart[2]) return 1;
-    return 2;
-}
-static int blk_bwd(const wlc_ctx* c, int s) {  // MDE_ABC.f90:69-83
-    if (s >= c->nstart[2]) return 2;
-    if (s >= c->nstart[1]) return 1;
-    return 0;
-}
-
-// Fill the launch description of one step.  h1..h3: history (or the RHS
-// for order 0), qout: destination slice.
-template <typename T>
-static StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h2, const T* h3, T* qout) {
-    using C = typename cvec<T>::t;
-    StepLaunch<T> L;
-    L.a_variant = c->a_variant;
-    L.solve_threads = c->solve_threads;
-    L.xy_threads = c->xy_threads;
-    L.xy_z = c->xy_z;
-    const size_t nr = (size_t)c->nr;
-    StepArgs<T>& a = L.step;
-    a.h1 = h1;
-    a.h2 = h2;
-    a.h3 = h3;
-    a.wb = c->w + (size_t)k.blk * nr;
-    a.cf = (const T*)c->cf + (size_t)k.blk * 3 * nr;
-    a.dsw = (const T*)c->cf + (size_t)(9 + k.blk) * nr;
-    a.third = (T)lit_third(c->real4);
-    a.msterm = nullptr;
-    a.order = k.order;
-    a.ds = (T)c->ds;
-    a.phat = (C*)c->phat;
-    a.twg = (const C*)c->twg;
-    a.M = c->M;
-    a.qout = qout;
-    a.minv = (T)(1.0 / (double)c->nr);  // M_grid_inv, wormlike_MDE_2dcomp_mod.f90:307
-    SolveArgs<T>& s = L.solve;
-    s.phat = (C*)c->phat;
-    s.twg = (const C*)c->twg;
-    if constexpr (sizeof(T) == 8)
-        s.tab = c->sd;
-    else
-        s.tab = c->sf;
-    for (int q = 0; q < 3; ++q) s.kf[q] = c->kf[q];
-    s.ds = c->ds;
-    s.sigma = k.sigma;
-    s.nkx = c->nkx;
-    s.correct = (!c->fp32 && s.tab.ndr > 0) ? 1 : 0;
-    s.npiv = c->npiv;
-    s.pivtab = nullptr;
-    if (c->have_piv && k.order >= 1 && k.order <= 3)
-        s.pivtab = (const T*)c->pivtab + ((size_t)((k.order - 1) * 3 + k.blk) * c->nkeys) * c->npiv;
-    // diagonal of G (Gmatrix_2dcomp_mod.f90:394): c0 + ds*Loa*l(l+1)/(2 kappa)
-    s.dcoef = c->ds * c->p.loa / (2.0 * c->p.kappa[k.blk]);
-    return L;
-}
-
 template <typename T> static int run_step(wlc_ctx* c, StepLaunch<T>& L, double c0, int slot) {
     L.solve.c0 = c0;
     L.events = (c->timing && slot >= 0) ? &c->ev[4 * (size_t)slot] : nullptr;
@@ -680,25 +488,6 @@ static int contour_step(wlc_ctx* c, StepKind k, const T* h1, const T* h2, const 
         L.step.msterm = (const T*)c->msterm;
     }
     return run_step<T>(c, L, lit_c0(k.order, c->real4), slot);
-}
-
-// slice addressing of the storage modes
-template <typename T> static T* qf_ring(wlc_ctx* c, int s) {
-    return (T*)c->qf + (size_t)(s & 3) * (size_t)c->M * c->nr;
-}
-template <typename T> static T* qf_ckpt(wlc_ctx* c, int m, int j) {  // q(mK - 2 + j), m >= 1
-    return (T*)c->qf + (size_t)(4 + 3 * (m - 1) + j) * (size_t)c->M * c->nr;
-}
-template <typename T> static T* qf_seg(wlc_ctx* c, int idx) {  // segment slot idx = s - mK + 2
-    return (T*)c->qf + (size_t)(4 + 3 * c->nck + idx) * (size_t)c->M * c->nr;
-}
-// q(s) as the backward sweep sees it
-template <typename T> static T* qf_at(wlc_ctx* c, int s) {
-    if (c->K == 0) return (T*)c->qf + (size_t)s * (size_t)c->M * c->nr;
-    return qf_seg<T>(c, s - (s / c->K) * c->K + 2);
-}
-template <typename T> static T* qb_at(wlc_ctx* c, int s) {
-    return (T*)c->qb + (size_t)(c->stream ? (s & 3) : s) * (size_t)c->M * c->nr;
 }
 
 // recompute q over segment m (slices mK+1 .. min(mK+K-1, Nmax)) into the
@@ -723,19 +512,6 @@ template <typename T> static int recompute_segment(wlc_ctx* c, int m) {
         if (rc) return rc;
     }
     return WLC_OK;
-}
-
-static DensityArgs density_args(const wlc_ctx* c) {
-    DensityArgs d;
-    d.nr = c->nr;
-    d.M = c->M;
-    d.nmax = c->p.nmax;
-    for (int b = 0; b < 3; ++b) {
-        d.nstart[b] = c->nstart[b];
-        d.ns[b] = c->p.ns[b];
-    }
-    d.ds = c->ds;
-    return d;
 }
 
 template <typename T> static int sweep(wlc_ctx* c, int dir) {
@@ -1214,31 +990,6 @@ extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, in
 // split only changes which thread owns which degree block / m system, and
 // both pass-A variants compute the same sums), so the tuner times them on
 // the instance's own data and keeps the fastest.
-static std::vector<int> solve_thread_candidates(int N) {
-    std::vector<int> out;
-    const int smax = std::max(1, kSolveThreads / N);
-    for (int S : {1, 2, 3, 4, 6, 8, 12, 16})
-        if (S <= smax) out.push_back(N * S);
-    if (out.empty() || out.back() != N * smax) out.push_back(N * smax);
-    return out;
-}
-
-template <typename F> static float time_ms(cudaStream_t st, F&& body, int reps) {
-    cudaEvent_t e0, e1;
-    cudaEventCreate(&e0);
-    cudaEventCreate(&e1);
-    body();  // warm-up
-    cudaEventRecord(e0, st);
-    for (int r = 0; r < reps; ++r) body();
-    cudaEventRecord(e1, st);
-    cudaEventSynchronize(e1);
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    return ms / (float)reps;
-}
-
 template <typename T> static int autotune_impl(wlc_ctx* c) {
     int rc;
     if (!c->have_fwd && (rc = sweep<T>(c, 1))) return rc;
@@ -1312,448 +1063,3 @@ extern "C" int wlc_set_launch_config(wlc_ctx* c, int32_t a_variant, int32_t solv
     c->xy_threads = xy_threads;
     return WLC_OK;
 }
-
-// ------------------------------------------------------------ batches
-// Several independent FP32 instances advanced together: one launch per pass
-// per grid-size group per contour step covers every instance of the group
-// (arguments from device arrays, instance = blockIdx.z), the streamed
-// density slices of all instances share one launch per step, and the whole
-// forward + backward contour loop is captured once into a CUDA graph and
-// replayed.
-struct wlc_batch {
-    std::vector<wlc_ctx*> inst;
-    cudaStream_t st = nullptr;
-    std::string err;
-    int nmax = 0, M = 0;
-    struct Group {
-        int N = 0;
-        std::vector<int> idx;
-        StepArgs<float>* dstep = nullptr;  // [2 directions][nmax + 1][count]
-        SolveArgs<float>* dsolve = nullptr;
-        size_t smem = 0;
-        int a_variant = 0, solve_threads = 0, xy_threads = 0, xy_z = 0;
-        std::vector<int> streamed;              // members with streamed densities
-        SliceBatchArgs<float>* dslice = nullptr;  // [streamed]
-        bool any_s = false;
-        cudaStream_t st = nullptr;  // the group's stream inside the captured contour loop
-        cudaEvent_t done = nullptr;
-    };
-    cudaEvent_t fork = nullptr;
-    std::vector<Group> groups;
-    std::vector<int> streamed;  // instances with streamed densities
-    std::vector<void*> allocs;
-    std::vector<long> sig;  // per instance: box generation and Maier-Saupe state at the last build
-    bool built = false;
-    bool use_graph = true;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t gexec = nullptr;
-    int64_t launches = 0;
-    int64_t per_replay = 0;  // kernel launches in one replay of the graph
-};
-
-static int bset_err(wlc_batch* b, int code, const std::string& msg) {
-    if (b) b->err = msg;
-    return code;
-}
-
-#define BCK(call)                                                                                         \
-    do {                                                                                                  \
-        cudaError_t e_ = (call);                                                                          \
-        if (e_ != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string(#call ": ") + cudaGetErrorString(e_)); \
-    } while (0)
-
-template <typename X> static int balloc(wlc_batch* b, X** p, size_t bytes) {
-    void* q = nullptr;
-    cudaError_t e = cudaMalloc(&q, bytes ? bytes : 16);
-    if (e != cudaSuccess) {
-        cudaGetLastError();
-        return bset_err(b, WLC_E_ALLOC, std::string("cudaMalloc: ") + cudaGetErrorString(e));
-    }
-    b->allocs.push_back(q);
-    *p = (X*)q;
-    return WLC_OK;
-}
-
-static void drop_graph(wlc_batch* b) {
-    if (b->gexec) cudaGraphExecDestroy(b->gexec);
-    if (b->graph) cudaGraphDestroy(b->graph);
-    b->gexec = nullptr;
-    b->graph = nullptr;
-}
-
-static bool ms_active(const wlc_ctx* c) { return std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop; }
-
-static std::vector<long> batch_signature(const wlc_batch* b) {
-    std::vector<long> v;
-    for (auto* c : b->inst) v.push_back(2L * c->box_gen + (ms_active(c) ? 1 : 0));
-    return v;
-}
-
-// history / output pointers of step n of direction dir for one instance
-static void step_ptrs(wlc_ctx* c, int dir, int n, const float** h, float** out, StepKind* k) {
-    const size_t sl = (size_t)c->M * c->nr;
-    const int nmax = c->p.nmax;
-    const int s = dir > 0 ? n : nmax - n;
-    const int order = n < 3 ? n : 3;
-    *k = StepKind{order, dir, dir > 0 ? blk_fwd(c, s) : blk_bwd(c, s)};
-    for (int j = 1; j <= 3; ++j) {
-        if (j > order) {
-            h[j - 1] = nullptr;
-            continue;
-        }
-        h[j - 1] = dir > 0 ? (const float*)c->qf + (size_t)(s - j) * sl : qb_at<float>(c, s + j);
-    }
-    *out = dir > 0 ? (float*)c->qf + (size_t)s * sl : qb_at<float>(c, s);
-}
-
-static int batch_build(wlc_batch* b) {
-    const int nmax = b->nmax;
-    for (auto& g : b->groups) {
-        const int cnt = (int)g.idx.size();
-        const size_t tot = (size_t)2 * (nmax + 1) * cnt;
-        std::vector<StepArgs<float>> hs(tot);
-        std::vector<SolveArgs<float>> hv(tot);
-        for (int d = 0; d < 2; ++d)
-            for (int n = 1; n <= nmax; ++n)
-                for (int j = 0; j < cnt; ++j) {
-                    wlc_ctx* c = b->inst[g.idx[j]];
-                    const float* h[3];
-                    float* out;
-                    StepKind k;
-                    step_ptrs(c, d == 0 ? 1 : -1, n, h, &out, &k);
-                    StepLaunch<float> L = make_launch<float>(c, k, h[0], h[1], h[2], out);
-                    L.solve.c0 = lit_c0(k.order, c->real4);
-                    if (ms_active(c)) L.step.msterm = (const float*)c->msterm;
-                    const size_t e = ((size_t)d * (nmax + 1) + n) * cnt + j;
-                    hs[e] = L.step;
-                    hv[e] = L.solve;
-                    const size_t sm = solve_smem_bytes<float>(L.solve);
-                    if (j == 0 && d == 0 && n == 1)
-                        g.smem = sm;
-                    else if (sm != g.smem)
-                        return bset_err(b, WLC_E_UNSUPPORTED, "instances of one grid size need one solve layout");
-                }
-        int rc;
-        if (!g.dstep) {
-            if ((rc = balloc(b, &g.dstep, sizeof(StepArgs<float>) * tot))) return rc;
-            if ((rc = balloc(b, &g.dsolve, sizeof(SolveArgs<float>) * tot))) return rc;
-        }
-        BCK(cudaMemcpy(g.dstep, hs.data(), sizeof(StepArgs<float>) * tot, cudaMemcpyHostToDevice));
-        BCK(cudaMemcpy(g.dsolve, hv.data(), sizeof(SolveArgs<float>) * tot, cudaMemcpyHostToDevice));
-    }
-    for (auto& g : b->groups) {
-        if (g.streamed.empty()) continue;
-        std::vector<SliceBatchArgs<float>> ha;
-        g.any_s = false;
-        for (int i : g.streamed) {
-            wlc_ctx* c = b->inst[i];
-            SliceBatchArgs<float> a;
-            a.qf = (const float*)c->qf;
-            a.qb = (const float*)c->qb;
-            a.sl = (int64_t)c->M * c->nr;
-            a.d = density_args(c);
-            a.want_s = stream_s(c) ? 1 : 0;
-            a.jl = c->jl;
-            a.raw = c->raw;
-            a.junc = c->junc;
-            a.qend = c->qend;
-            a.sraw = c->sraw;
-            g.any_s = g.any_s || a.want_s;
-            ha.push_back(a);
-        }
-        int rc;
-        if (!g.dslice && (rc = balloc(b, &g.dslice, sizeof(SliceBatchArgs<float>) * ha.size()))) return rc;
-        BCK(cudaMemcpy(g.dslice, ha.data(), sizeof(SliceBatchArgs<float>) * ha.size(), cudaMemcpyHostToDevice));
-    }
-    b->sig = batch_signature(b);
-    b->built = true;
-    return WLC_OK;
-}
-
-// enqueue the forward and backward sweeps of one grid-size group on stream st
-static int batch_issue_group(wlc_batch* b, wlc_batch::Group& g, cudaStream_t st) {
-    const int nmax = b->nmax;
-    const int cnt = (int)g.idx.size();
-    auto step = [&](int d, int n) -> int {
-        const int dir = d == 0 ? 1 : -1;
-        for (int i : g.idx) {
-            wlc_ctx* c = b->inst[i];
-            if (!ms_active(c)) continue;
-            const float* h[3];
-            float* out;
-            StepKind k;
-            step_ptrs(c, dir, n, h, &out, &k);
-            launch_ms_term<float>(h[0], h[1], h[2], k.order, c->mop, c->thl, c->ds, lit_thresh(c->real4), c->M,
-                                  c->nr, (float*)c->msterm, st);
-            b->launches++;
-        }
-        BatchLaunch<float> bl;
-        const size_t e = ((size_t)d * (nmax + 1) + n) * cnt;
-        bl.dstep = g.dstep + e;
-        bl.dsolve = g.dsolve + e;
-        bl.count = cnt;
-        bl.M = b->M;
-        bl.nkx = g.N / 2 + 1;
-        bl.solve_smem = g.smem;
-        bl.a_variant = g.a_variant;
-        bl.solve_threads = g.solve_threads;
-        bl.xy_threads = g.xy_threads;
-        bl.xy_z = g.xy_z;
-        cudaError_t err = launch_step_batched(g.N, bl, st);
-        b->launches += 3;
-        if (err != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("batched step: ") + cudaGetErrorString(err));
-        return WLC_OK;
-    };
-    auto slices = [&](int s) {
-        if (g.streamed.empty()) return;
-        const wlc_ctx* c0 = b->inst[g.streamed[0]];
-        launch_density_slice_batched<float>(g.dslice, (int)g.streamed.size(), c0->nr, s, b->M, c0->jl.n,
-                                            g.any_s ? 1 : 0, st);
-        b->launches++;
-    };
-    int rc;
-    for (int i : g.idx) {
-        wlc_ctx* c = b->inst[i];
-        launch_set_delta<float>((float*)c->qf, c->M, c->nr, st);
-        b->launches++;
-    }
-    for (int n = 1; n <= nmax; ++n)
-        if ((rc = step(0, n))) return rc;
-    for (int i : g.streamed) {
-        wlc_ctx* c = b->inst[i];
-        BCK(cudaMemsetAsync(c->raw, 0, sizeof(double) * 3 * (size_t)c->nr, st));
-        if (stream_s(c)) BCK(cudaMemsetAsync(c->sraw, 0, sizeof(double) * 15 * (size_t)c->nr, st));
-    }
-    for (int i : g.idx) {
-        wlc_ctx* c = b->inst[i];
-        launch_set_delta<float>(qb_at<float>(c, nmax), c->M, c->nr, st);
-        b->launches++;
-    }
-    slices(nmax);
-    for (int n = 1; n <= nmax; ++n) {
-        if ((rc = step(1, n))) return rc;
-        slices(nmax - n);
-    }
-    BCK(cudaGetLastError());
-    return WLC_OK;
-}
-
-// enqueue the sweeps of every instance: the groups are independent, so each
-// runs on its own stream (forked from and joined back into the batch
-// stream; inside stream capture this becomes parallel branches of the graph)
-static int batch_issue(wlc_batch* b) {
-    if (b->groups.size() == 1) return batch_issue_group(b, b->groups[0], b->st);
-    BCK(cudaEventRecord(b->fork, b->st));
-    int rc = WLC_OK;
-    for (auto& g : b->groups) {
-        BCK(cudaStreamWaitEvent(g.st, b->fork, 0));
-        if ((rc = batch_issue_group(b, g, g.st))) break;
-        BCK(cudaEventRecord(g.done, g.st));
-    }
-    for (auto& g : b->groups) BCK(cudaStreamWaitEvent(b->st, g.done, 0));
-    return rc;
-}
-
-extern "C" int wlc_batch_create(const wlc_params* p, int32_t count, wlc_batch** out) {
-    if (!p || !out || count < 1) return WLC_E_PARAM;
-    wlc_batch* b = new wlc_batch();
-    *out = b;
-    for (int i = 0; i < count; ++i) {
-        const wlc_params& q = p[i];
-        char buf[200];
-        if (q.precision != WLC_FP32 || !supported_batch_n(q.n[0]) || q.q_checkpoint != 0 || q.nmax != p[0].nmax ||
-            q.lmax != p[0].lmax) {
-            std::snprintf(buf, sizeof buf,
-                          "instance %d: batches take FP32 instances with one nmax and lmax, no q_checkpoint, and a "
-                          "grid edge in {16, 24, 32, 40, 48, 64}",
-                          i);
-            return bset_err(b, WLC_E_UNSUPPORTED, buf);
-        }
-    }
-    b->nmax = p[0].nmax;
-    b->M = (p[0].lmax + 1) * (p[0].lmax + 1);
-    BCK(cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking));
-    for (int i = 0; i < count; ++i) {
-        wlc_ctx* c = nullptr;
-        int rc = create_impl(&p[i], b->st, &c);
-        if (rc) {
-            b->err = "instance " + std::to_string(i) + ": " + (c ? c->err : std::string("create failed"));
-            if (c) destroy_impl(c);
-            return rc;
-        }
-        c->batch_owned = true;
-        b->inst.push_back(c);
-        bool found = false;
-        for (auto& g : b->groups)
-            if (g.N == c->N) {
-                g.idx.push_back(i);
-                found = true;
-            }
-        if (!found) {
-            wlc_batch::Group g;
-            g.N = c->N;
-            g.idx.push_back(i);
-            b->groups.push_back(g);
-        }
-        if (c->stream) {
-            b->streamed.push_back(i);
-            for (auto& g : b->groups)
-                if (g.N == c->N) g.streamed.push_back(i);
-        }
-    }
-    for (auto& g : b->groups) {
-        BCK(prepare_step_batched(g.N));
-        BCK(cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking));
-        BCK(cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming));
-    }
-    BCK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-    return WLC_OK;
-}
-
-extern "C" int wlc_batch_destroy(wlc_batch* b) {
-    if (!b) return WLC_OK;
-    if (b->st) cudaStreamSynchronize(b->st);
-    drop_graph(b);
-    for (auto* c : b->inst) destroy_impl(c);
-    for (void* q : b->allocs) cudaFree(q);
-    for (auto& g : b->groups) {
-        if (g.st) {
-            cudaStreamSynchronize(g.st);
-            cudaStreamDestroy(g.st);
-        }
-        if (g.done) cudaEventDestroy(g.done);
-    }
-    if (b->fork) cudaEventDestroy(b->fork);
-    if (b->st) cudaStreamDestroy(b->st);
-    delete b;
-    return WLC_OK;
-}
-
-extern "C" const char* wlc_batch_last_error(const wlc_batch* b) { return b ? b->err.c_str() : "null batch"; }
-
-extern "C" int32_t wlc_batch_size(const wlc_batch* b) { return b ? (int32_t)b->inst.size() : 0; }
-
-extern "C" int wlc_batch_get(wlc_batch* b, int32_t i, wlc_ctx** ctx) {
-    if (!b || !ctx || i < 0 || i >= (int)b->inst.size()) return bset_err(b, WLC_E_PARAM, "bad instance index");
-    *ctx = b->inst[i];
-    return WLC_OK;
-}
-
-extern "C" void* wlc_batch_stream(const wlc_batch* b) { return b ? (void*)b->st : nullptr; }
-
-extern "C" int64_t wlc_batch_launch_count(const wlc_batch* b) { return b ? b->launches : 0; }
-
-extern "C" int wlc_batch_use_graph(wlc_batch* b, int32_t on) {
-    if (!b) return WLC_E_PARAM;
-    b->use_graph = on != 0;
-    drop_graph(b);
-    return WLC_OK;
-}
-
-extern "C" int wlc_batch_propagate(wlc_batch* b) {
-    if (!b || !b->st) return WLC_E_STATE;
-    for (auto* c : b->inst)
-        if (!c->have_fields) return bset_err(b, WLC_E_STATE, "every instance needs wlc_set_fields first");
-    for (auto* c : b->inst)
-        if (c->fp32 == false) return bset_err(b, WLC_E_STATE, "batch instances must stay FP32");
-    int rc;
-    if (!b->built || b->sig != batch_signature(b)) {
-        drop_graph(b);
-        if ((rc = batch_build(b))) return rc;
-    }
-    if (b->use_graph) {
-        if (!b->gexec) {
-            BCK(cudaStreamSynchronize(b->st));
-            BCK(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
-            const int64_t l0 = b->launches;
-            rc = batch_issue(b);
-            cudaGraph_t gr = nullptr;
-            cudaError_t e = cudaStreamEndCapture(b->st, &gr);
-            if (rc) {
-                if (gr) cudaGraphDestroy(gr);
-                return rc;
-            }
-            if (e != cudaSuccess) return bset_err(b, WLC_E_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-            b->graph = gr;
-            BCK(cudaGraphInstantiate(&b->gexec, b->graph, 0));
-            b->per_replay = b->launches - l0;
-            b->launches = l0;  // counted per replay below
-        }
-        BCK(cudaGraphLaunch(b->gexec, b->st));
-        b->launches += b->per_replay;
-    } else {
-        if ((rc = batch_issue(b))) return rc;
-    }
-    for (auto* c : b->inst) {
-        c->have_fwd = c->have_bwd = true;
-        c->have_density = false;
-    }
-    return WLC_OK;
-}
-
-// Time the batched step of each grid-size group under every candidate
-// launch configuration (on the last forward step, which re-runs with the
-// same inputs and output) and keep the fastest; the graph is re-captured.
-extern "C" int wlc_batch_autotune(wlc_batch* b, int32_t* config) {
-    if (!b || !b->st) return WLC_E_STATE;
-    int rc;
-    if ((rc = wlc_batch_propagate(b))) return rc;
-    const int nmax = b->nmax;
-    for (size_t gi = 0; gi < b->groups.size(); ++gi) {
-        auto& g = b->groups[gi];
-        const int cnt = (int)g.idx.size();
-        float best = 1e30f;
-        int best_a = g.a_variant, best_t = g.solve_threads, best_x = g.xy_threads, best_z = g.xy_z;
-        for (int xz : {0, 1})
-        for (int xt : {256, 512})
-        for (int av : {1, 2})
-            for (int th : solve_thread_candidates(g.N)) {
-                BatchLaunch<float> bl;
-                const size_t e = (size_t)nmax * cnt;  // direction 0, step nmax
-                bl.dstep = g.dstep + e;
-                bl.dsolve = g.dsolve + e;
-                bl.count = cnt;
-                bl.M = b->M;
-                bl.nkx = g.N / 2 + 1;
-                bl.solve_smem = g.smem;
-                bl.a_variant = av;
-                bl.solve_threads = th;
-                bl.xy_threads = xt;
-                bl.xy_z = xz;
-                for (int i : g.idx) {  // Theta terms of that step
-                    wlc_ctx* c = b->inst[i];
-                    if (!ms_active(c)) continue;
-                    const float* h[3];
-                    float* out;
-                    StepKind k;
-                    step_ptrs(c, 1, nmax, h, &out, &k);
-                    launch_ms_term<float>(h[0], h[1], h[2], k.order, c->mop, c->thl, c->ds, lit_thresh(c->real4),
-                                          c->M, c->nr, (float*)c->msterm, b->st);
-                }
-                const float t = time_ms(b->st, [&] { launch_step_batched(g.N, bl, b->st); }, 3);
-                BCK(cudaGetLastError());
-                if (t < best) {
-                    best = t;
-                    best_a = av;
-                    best_t = th;
-                    best_x = xt;
-                    best_z = xz;
-                }
-            }
-        g.a_variant = best_a;
-        g.solve_threads = best_t;
-        g.xy_threads = best_x;
-        g.xy_z = best_z;
-        if (config) {
-            config[5 * gi] = g.N;
-            config[5 * gi + 1] = best_a;
-            config[5 * gi + 2] = best_t;
-            config[5 * gi + 3] = best_x;
-            config[5 * gi + 4] = best_z;
-        }
-    }
-    drop_graph(b);
-    return WLC_OK;
-}
-
-extern "C" int32_t wlc_batch_groups(const wlc_batch* b) { return b ? (int32_t)b->groups.size() : 0; }
