@@ -376,7 +376,7 @@ def run_ours(args, wl):
                            "precision": wl["precision"], "l2": "inputs larger than L2 (51 GB history/direction)",
                            "parallelism": "replicas" if world > 1 else "single",
                            "launch_config": {"a_variant": tuned[0], "solve_threads": tuned[1],
-                                             "xy_threads": tuned[2], "xy_half_planes": tuned[3]} if tuned else
+                                             "xy_threads": tuned[2], "xy_variant": tuned[3]} if tuned else
                            "default"},
                 "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clocks,
@@ -864,7 +864,7 @@ def main():
     ap.add_argument("--count", type=int, default=48, help="instances of the batched workload")
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration")
     ap.add_argument("--no-fp32", action="store_true", help="fp64 run: skip the FP32 form's line entry")
-    ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads[,xy_threads[,xy_half_planes]]")
+    ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads[,xy_threads[,xy_variant]]")
     ap.add_argument("--forms", default="fp32sched,fp64")
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--switch-tol", type=float, default=1e-4)

@@ -220,13 +220,14 @@ int wlc_last_timing(const wlc_ctx* ctx, double* ms4);
  * (pass A variant, threads per solve CTA; all give identical results) and
  * keep the fastest.  Runs a forward sweep first if none is current.
  * config (may be NULL) receives {a_variant, solve_threads, xy_threads,
- * xy_half_planes} (pass A variant 1 generic / 2 staged; threads per solve
- * CTA; threads per CTA of the generic pass A and pass C, 256 or 512; 1 when
- * those CTAs take half the default number of z planes).
+ * xy_variant} (pass A variant 1 generic / 2 staged; threads per solve CTA;
+ * threads per CTA of the generic pass A and pass C, 256 or 512; their
+ * variant: bit 0 half the default number of z planes per CTA, bit 1 the
+ * x-FFTs of all planes in one batched call).
  * wlc_set_launch_config sets them by hand (0, 0, 0, 0 = defaults). */
 int wlc_autotune(wlc_ctx* ctx, int32_t* config);
 int wlc_set_launch_config(wlc_ctx* ctx, int32_t a_variant, int32_t solve_threads, int32_t xy_threads,
-                          int32_t xy_half_planes);
+                          int32_t xy_variant);
 
 /* No counterpart in the reference (one instance per MPI job there).
  * Batches: independent FP32 instances (own grid, box, composition, chi,
@@ -249,7 +250,7 @@ int wlc_batch_get(wlc_batch* b, int32_t i, wlc_ctx** ctx);
 /* MDE_q and MDE_qstar of every instance (wormlike_MDE_2dcomp_mod.f90:231-1557
  * per instance); the graph is re-captured after a box or Maier-Saupe change. */
 int wlc_batch_propagate(wlc_batch* b);
-/* per grid-size group: config[5g..5g+4] = {N, a_variant, solve_threads, xy_threads, xy_half_planes}
+/* per grid-size group: config[5g..5g+4] = {N, a_variant, solve_threads, xy_threads, xy_variant}
  * (may be NULL) */
 int wlc_batch_autotune(wlc_batch* b, int32_t* config);
 int wlc_batch_use_graph(wlc_batch* b, int32_t on);  /* 0: issue the launches directly */

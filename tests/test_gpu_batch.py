@@ -112,7 +112,7 @@ def test_batch_autotune_keeps_results():
     b.propagate()
     before = [inst.density(want_junction=False) for inst in b.instances]
     cfg = b.autotune()
-    assert sorted(c[0] for c in cfg) == [16, 24] and all(c[3] in (256, 512) and c[4] in (0, 1) for c in cfg)
+    assert sorted(c[0] for c in cfg) == [16, 24] and all(c[3] in (256, 512) and 0 <= c[4] <= 3 for c in cfg)
     b.propagate()
     for inst, d0 in zip(b.instances, before):
         d = inst.density(want_junction=False)
@@ -138,13 +138,13 @@ def test_single_autotune_keeps_results(precision):
     g.MDE_q()
     g.MDE_qstar()
     d0 = g.density()
-    a_var, threads, xy, half = g.autotune()
-    assert a_var in (1, 2) and threads % n == 0 and 0 < threads <= 256 and xy in (256, 512) and half in (0, 1)
+    a_var, threads, xy, xv = g.autotune()
+    assert a_var in (1, 2) and threads % n == 0 and 0 < threads <= 256 and xy in (256, 512) and 0 <= xv <= 3
     g.MDE_q()
     g.MDE_qstar()
     d = g.density()
     assert d["lnQ"] == d0["lnQ"] and np.array_equal(d["phi"], d0["phi"])
-    for cfg in ((1, n, 512, 1), (2, 2 * n, 256, 0), (1, 3 * n, 512, 0), (1, 2 * n, 256, 1), (0, 0, 0, 0)):
+    for cfg in ((1, n, 512, 1), (2, 2 * n, 256, 0), (1, 3 * n, 512, 2), (1, 2 * n, 256, 3), (0, 0, 0, 0)):
         g.set_launch_config(*cfg)
         g.MDE_q()
         g.MDE_qstar()

@@ -1002,7 +1002,7 @@ template <typename T> static int autotune_impl(wlc_ctx* c) {
     float best = 1e30f;
     int best_a = c->a_variant, best_t = c->solve_threads, best_x = c->xy_threads, best_z = c->xy_z;
     const bool ms = std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop;
-    for (int xz : {0, 1})
+    for (int xz : {0, 1, 2, 3})
     for (int xt : {256, 512})
     for (int av : {1, 2}) {
         if (av == 2 && sizeof(T) != 4) continue;
@@ -1051,13 +1051,13 @@ extern "C" int wlc_autotune(wlc_ctx* c, int32_t* config) {
 }
 
 extern "C" int wlc_set_launch_config(wlc_ctx* c, int32_t a_variant, int32_t solve_threads, int32_t xy_threads,
-                                     int32_t xy_half_planes) {
+                                     int32_t xy_variant) {
     if (!ready(c)) return WLC_E_STATE;
     if (a_variant < 0 || a_variant > 2 || solve_threads < 0 || solve_threads > kSolveThreads ||
-        (xy_threads != 0 && xy_threads != 256 && xy_threads != 512) || xy_half_planes < 0 || xy_half_planes > 1)
+        (xy_threads != 0 && xy_threads != 256 && xy_threads != 512) || xy_variant < 0 || xy_variant > 3)
         return set_err(c, WLC_E_PARAM,
-                       "a_variant must be 0..2, solve_threads 0..256, xy_threads 0, 256 or 512, xy_half_planes 0 or 1");
-    c->xy_z = xy_half_planes;
+                       "a_variant must be 0..2, solve_threads 0..256, xy_threads 0, 256 or 512, xy_variant 0..3");
+    c->xy_z = xy_variant;
     c->a_variant = a_variant;
     c->solve_threads = solve_threads;
     c->xy_threads = xy_threads;

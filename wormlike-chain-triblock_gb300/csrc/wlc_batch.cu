@@ -395,7 +395,7 @@ extern "C" int wlc_batch_autotune(wlc_batch* b, int32_t* config) {
         const int cnt = (int)g.idx.size();
         float best = 1e30f;
         int best_a = g.a_variant, best_t = g.solve_threads, best_x = g.xy_threads, best_z = g.xy_z;
-        for (int xz : {0, 1})
+        for (int xz : {0, 1, 2, 3})
         for (int xt : {256, 512})
         for (int av : {1, 2})
             for (int th : solve_thread_candidates(g.N)) {

@@ -90,20 +90,23 @@ template <int n> __device__ __forceinline__ void cp_async_wait() {
 // The half-spectrum planes of a CTA are kept z-fastest, out[(ky*NKX + kx)*Z + zz],
 // so that the Z values of one (col, i) run in phat move as one 32-byte chunk.
 
-// x-FFT of packed row pairs, split into two half spectra; plane zz of out
-// (the y-FFTs of all planes follow in one batched call, fwd_y_planes)
-template <typename T, int N, int Z>
-__device__ __forceinline__ void fwd_x_plane(typename cvec<T>::t* zb, typename cvec<T>::t* out, int zz,
-                                            const typename cvec<T>::t* tw) {
+// x-FFTs of ZB planes of packed row pairs (zb: ZB consecutive (N/2) x N
+// blocks), split into two half spectra each: planes zz0 .. zz0+ZB-1 of out
+// (the y-FFTs of all planes follow in one batched call, y_planes)
+template <typename T, int N, int Z, int ZB>
+__device__ __forceinline__ void fwd_x_planes(typename cvec<T>::t* zb, typename cvec<T>::t* out, int zz0,
+                                             const typename cvec<T>::t* tw) {
     using C = typename cvec<T>::t;
     constexpr int NKX = N / 2 + 1;
-    fft_nat2perm<N, -1>(zb, N / 2, 1, N, tw);
-    for (int e = threadIdx.x; e < (N / 2) * NKX; e += blockDim.x) {
+    fft_nat2perm<N, -1>(zb, ZB * (N / 2), 1, N, tw);
+    for (int t = threadIdx.x; t < ZB * (N / 2) * NKX; t += blockDim.x) {
+        const int q = t / ((N / 2) * NKX), e = t % ((N / 2) * NKX);
         const int p = e / NKX, k = e % NKX;
-        const C zk = zb[p * N + perm_pos<N>(k)];
-        const C zm = zb[p * N + perm_pos<N>((N - k) % N)];
-        out[((2 * p) * NKX + k) * Z + zz] = cmk<C>((T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y - zm.y));
-        out[((2 * p + 1) * NKX + k) * Z + zz] = cmk<C>((T)0.5 * (zk.y + zm.y), (T)0.5 * (zm.x - zk.x));
+        const C* zq = zb + (size_t)q * (N / 2) * N;
+        const C zk = zq[p * N + perm_pos<N>(k)];
+        const C zm = zq[p * N + perm_pos<N>((N - k) % N)];
+        out[((2 * p) * NKX + k) * Z + zz0 + q] = cmk<C>((T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y - zm.y));
+        out[((2 * p + 1) * NKX + k) * Z + zz0 + q] = cmk<C>((T)0.5 * (zk.y + zm.y), (T)0.5 * (zm.x - zk.x));
     }
     __syncthreads();
 }
@@ -131,46 +134,55 @@ __device__ __forceinline__ void store_phat(const StepArgs<T>& a, const typename 
 }
 
 // ---------------------------------------------------------------- pass A
-template <typename T, int N, bool B = false, int ZD = 0>
+// V: launch variant, bit 0 half the planes per CTA, bit 1 the x-FFTs of all
+// planes in one batched call (one packed-row buffer per plane)
+template <typename T, int N, int V> struct XyShape {
+    static constexpr int Z = xy_planes(N, sizeof(T), V & 1);
+    static constexpr int ZB = (V & 2) ? Z : 1;
+};
+
+template <typename T, int N, bool B = false, int V = 0>
 __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
     const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
-    constexpr int Z = xy_planes(N, sizeof(T), ZD);
+    constexpr int Z = XyShape<T, N, V>::Z, ZB = XyShape<T, N, V>::ZB;
     constexpr int NR = N * N * N;
+    constexpr int PB = (N / 2) * N;  // packed row pairs per plane
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
-    C* zb = tw + N;              // (N/2) x N packed row pairs
-    C* out = zb + (N / 2) * N;   // N x NKX x Z half spectra
+    C* zb = tw + N;                  // ZB x (N/2) x N packed row pairs
+    C* out = zb + (size_t)ZB * PB;   // N x NKX x Z half spectra
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
-    for (int zz = 0; zz < Z; ++zz) {
-        const int z = z0 + zz;
+    for (int zz0 = 0; zz0 < Z; zz0 += ZB) {
         if constexpr (sizeof(T) == 4) {
             // four consecutive x per thread: 16-byte loads of the history, ds*w
             // and Theta planes (N is a multiple of 4)
-            for (int e4 = threadIdx.x; e4 < (N / 2) * N / 4; e4 += blockDim.x) {
-                const int e = 4 * e4;
+            for (int t = threadIdx.x; t < ZB * PB / 4; t += blockDim.x) {
+                const int q = t / (PB / 4), e = 4 * (t % (PB / 4));
                 const int p = e / N, x = e % N;
-                const size_t ra = ((size_t)z * N + 2 * p) * N + x, rb = ra + N;
+                const size_t ra = ((size_t)(z0 + zz0 + q) * N + 2 * p) * N + x, rb = ra + N;
                 const float4 va = rhs_f32x4(a, (size_t)i * NR + ra, ra);
                 const float4 vb = rhs_f32x4(a, (size_t)i * NR + rb, rb);
-                zb[e] = cmk<C>(va.x, vb.x);
-                zb[e + 1] = cmk<C>(va.y, vb.y);
-                zb[e + 2] = cmk<C>(va.z, vb.z);
-                zb[e + 3] = cmk<C>(va.w, vb.w);
+                C* zq = zb + (size_t)q * PB + e;
+                zq[0] = cmk<C>(va.x, vb.x);
+                zq[1] = cmk<C>(va.y, vb.y);
+                zq[2] = cmk<C>(va.z, vb.z);
+                zq[3] = cmk<C>(va.w, vb.w);
             }
         } else {
-            for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
+            for (int t = threadIdx.x; t < ZB * PB; t += blockDim.x) {
+                const int q = t / PB, e = t % PB;
                 const int p = e / N, x = e % N;
-                const size_t ra = ((size_t)z * N + 2 * p) * N + x, rb = ra + N;
+                const size_t ra = ((size_t)(z0 + zz0 + q) * N + 2 * p) * N + x, rb = ra + N;
                 const T va = rhs_value<T, NR>(a, (size_t)i * NR + ra, ra);
                 const T vb = rhs_value<T, NR>(a, (size_t)i * NR + rb, rb);
-                zb[e] = cmk<C>(va, vb);
+                zb[(size_t)q * PB + e] = cmk<C>(va, vb);
             }
         }
         __syncthreads();
-        fwd_x_plane<T, N, Z>(zb, out, zz, tw);
+        fwd_x_planes<T, N, Z, ZB>(zb, out, zz0, tw);
     }
     y_planes<T, N, Z, -1>(out, tw);
     store_phat<T, N, Z>(a, out, i, z0);
@@ -248,24 +260,25 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
             zb[e] = make_float2(va, vb);
         }
         __syncthreads();
-        fwd_x_plane<float, N, Z>(zb, out, zz, tw);
+        fwd_x_planes<float, N, Z, 1>(zb, out, zz, tw);
     }
     y_planes<float, N, Z, -1>(out, tw);
     store_phat<float, N, Z>(a, out, i, z0);
 }
 
 // ---------------------------------------------------------------- pass C
-template <typename T, int N, bool B = false, int ZD = 0>
+template <typename T, int N, bool B = false, int V = 0>
 __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>* __restrict__ batch) {
     const StepArgs<T> a = pick_args<B>(a0, batch);
     using C = typename cvec<T>::t;
-    constexpr int Z = xy_planes(N, sizeof(T), ZD);
+    constexpr int Z = XyShape<T, N, V>::Z, ZB = XyShape<T, N, V>::ZB;
     constexpr int NKX = N / 2 + 1;
     constexpr int NR = N * N * N;
+    constexpr int PB = (N / 2) * N;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
     C* zb = tw + N;
-    C* out = zb + (N / 2) * N;
+    C* out = zb + (size_t)ZB * PB;
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
@@ -282,10 +295,12 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
     cp_async_wait<0>();
     __syncthreads();
     y_planes<T, N, Z, +1>(out, tw);  // along y for every plane; row y now at perm_pos(y)
-    for (int zz = 0; zz < Z; ++zz) {
+    for (int zz0 = 0; zz0 < Z; zz0 += ZB) {
         // Hermitian extension of rows (2p, 2p+1) packed as one complex row;
         // the imaginary parts at kx = 0 and N/2 are discarded (c2r)
-        for (int e = threadIdx.x; e < (N / 2) * N; e += blockDim.x) {
+        for (int t = threadIdx.x; t < ZB * PB; t += blockDim.x) {
+            const int q = t / PB, e = t % PB;
+            const int zz = zz0 + q;
             const int p = e / N, k = e % N;
             const C* ra = out + (size_t)perm_pos<N>(2 * p) * NKX * Z + zz;
             const C* rb = out + (size_t)perm_pos<N>(2 * p + 1) * NKX * Z + zz;
@@ -303,15 +318,15 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
                 xa.y = -xa.y;
                 xb.y = -xb.y;
             }
-            zb[e] = cmk<C>(xa.x - xb.y, xa.y + xb.x);
+            zb[t] = cmk<C>(xa.x - xb.y, xa.y + xb.x);
         }
         __syncthreads();
-        fft_nat2perm<N, +1>(zb, N / 2, 1, N, tw);  // along x; x at perm_pos(x)
-        T* dst = a.qout + (size_t)i * NR + (size_t)(z0 + zz) * N * N;
-        for (int e = threadIdx.x; e < N * N; e += blockDim.x) {
+        fft_nat2perm<N, +1>(zb, ZB * (N / 2), 1, N, tw);  // along x; x at perm_pos(x)
+        for (int t = threadIdx.x; t < ZB * N * N; t += blockDim.x) {
+            const int q = t / (N * N), e = t % (N * N);
             const int y = e / N, x = e % N;
-            const C v = zb[(y >> 1) * N + perm_pos<N>(x)];
-            dst[e] = ((y & 1) ? v.y : v.x) * a.minv;
+            const C v = zb[(size_t)q * PB + (y >> 1) * N + perm_pos<N>(x)];
+            a.qout[(size_t)i * NR + (size_t)(z0 + zz0 + q) * N * N + e] = ((y & 1) ? v.y : v.x) * a.minv;
         }
         __syncthreads();
     }
@@ -327,9 +342,10 @@ __global__ void __launch_bounds__(256) rhs_only(StepArgs<T> a, T* out) {
 }
 
 // ------------------------------------------------------------ launchers
-template <typename T> size_t smem_xy(int N, int zd) {
+template <typename T> size_t smem_xy(int N, int variant) {
     using C = typename cvec<T>::t;
-    return sizeof(C) * ((size_t)N + (size_t)(N / 2) * N + (size_t)xy_planes(N, sizeof(T), zd) * N * (N / 2 + 1));
+    const int z = xy_planes(N, sizeof(T), variant & 1), zb = (variant & 2) ? z : 1;
+    return sizeof(C) * ((size_t)N + (size_t)zb * (N / 2) * N + (size_t)z * N * (N / 2 + 1));
 }
 
 template <typename T, int N, bool B> static void set_xy_attrs() {
@@ -339,6 +355,14 @@ template <typename T, int N, bool B> static void set_xy_attrs() {
     cudaFuncSetAttribute(ifft_xy<T, N, B, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(ifft_xy<T, N, B, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (smem_xy<T>(N, 2) <= 200 * 1024) {
+        cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(ifft_xy<T, N, B, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    }
+    if (smem_xy<T>(N, 3) <= 200 * 1024) {
+        cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaFuncSetAttribute(ifft_xy<T, N, B, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    }
     if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
         cudaFuncSetAttribute(rhs_fft_xy_staged<N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)StagedA<N>::bytes);
@@ -356,26 +380,30 @@ template <typename T, int N> static bool use_staged(int variant) {
         return false;
 }
 
-// generic pass A / pass C launches in plane variant ZD
-template <typename T, int N, bool B, int ZD>
-static void launch_xy(bool do_a, bool do_c_only, const StepArgs<T>& a, const StepArgs<T>* batch, int M, int count,
-                      int threads, cudaStream_t st) {
-    constexpr int Z = xy_planes(N, sizeof(T), ZD);
-    const size_t sxy = smem_xy<T>(N, ZD);
+// generic pass A / pass C launches in variant V (bit 0 half planes, bit 1
+// batched x-FFTs)
+template <typename T, int N, bool B, int V>
+static void launch_xy(bool do_a, const StepArgs<T>& a, const StepArgs<T>* batch, int M, int count, int threads,
+                      cudaStream_t st) {
+    constexpr int Z = XyShape<T, N, V>::Z;
+    const size_t sxy = smem_xy<T>(N, V);
     const dim3 g(N / Z, M, count);
     if (do_a)
-        rhs_fft_xy<T, N, B, ZD><<<g, xy_block(threads), sxy, st>>>(a, batch);
-    else if (do_c_only)
-        ifft_xy<T, N, B, ZD><<<g, xy_block(threads), sxy, st>>>(a, batch);
+        rhs_fft_xy<T, N, B, V><<<g, xy_block(threads), sxy, st>>>(a, batch);
+    else
+        ifft_xy<T, N, B, V><<<g, xy_block(threads), sxy, st>>>(a, batch);
 }
 
 template <typename T, int N, bool B>
-static void launch_xy_any(int zd, bool do_a, const StepArgs<T>& a, const StepArgs<T>* batch, int M, int count,
+static void launch_xy_any(int variant, bool do_a, const StepArgs<T>& a, const StepArgs<T>* batch, int M, int count,
                           int threads, cudaStream_t st) {
-    if (zd == 1)
-        launch_xy<T, N, B, 1>(do_a, !do_a, a, batch, M, count, threads, st);
-    else
-        launch_xy<T, N, B, 0>(do_a, !do_a, a, batch, M, count, threads, st);
+    if ((variant & 2) && smem_xy<T>(N, variant) > 200 * 1024) variant &= 1;  // batched x-FFTs do not fit
+    switch (variant & 3) {
+        case 1: launch_xy<T, N, B, 1>(do_a, a, batch, M, count, threads, st); break;
+        case 2: launch_xy<T, N, B, 2>(do_a, a, batch, M, count, threads, st); break;
+        case 3: launch_xy<T, N, B, 3>(do_a, a, batch, M, count, threads, st); break;
+        default: launch_xy<T, N, B, 0>(do_a, a, batch, M, count, threads, st); break;
+    }
 }
 
 template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s, cudaStream_t st) {

@@ -374,14 +374,14 @@ class Instance:
     def autotune(self):
         """Time the launch configurations of a contour step on this
         instance's data and keep the fastest; returns (a_variant,
-        solve_threads, xy_threads, xy_half_planes)."""
+        solve_threads, xy_threads, xy_variant)."""
         cfg = (ctypes.c_int32 * 4)()
         self._check(self.lib.wlc_autotune(self.h, cfg))
         return tuple(int(v) for v in cfg)
 
-    def set_launch_config(self, a_variant=0, solve_threads=0, xy_threads=0, xy_half_planes=0):
+    def set_launch_config(self, a_variant=0, solve_threads=0, xy_threads=0, xy_variant=0):
         self._check(self.lib.wlc_set_launch_config(self.h, int(a_variant), int(solve_threads), int(xy_threads),
-                                                   int(xy_half_planes)))
+                                                   int(xy_variant)))
 
     def reset_mixing(self):
         self._check(self.lib.wlc_reset_mixing(self.h))
