@@ -121,10 +121,10 @@ __device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, 
         if (!((mmask >> m) & 1u)) continue;
         const int n = L - m + 1;
         T dinv[16];
-        if (pivrow) {
-            const T* pr = pivrow + m * (L + 1) - (m * (m - 1)) / 2;
-            for (int j = 0; j < n; ++j) dinv[j] = pr[j];
-        } else {
+        // with a pivot table the inverse pivots are read from its row (L1-resident)
+        // rather than copied into a runtime-indexed local array
+        const T* pr = pivrow ? pivrow + m * (L + 1) - (m * (m - 1)) / 2 : dinv;
+        if (!pivrow) {
             T d = c0 + dcoef * (T)(m * (m + 1));
             dinv[0] = (T)1 / d;
             for (int j = 1; j < n; ++j) {
@@ -143,20 +143,20 @@ __device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, 
                 const int l = m + j;
                 const int prev = idx;
                 idx = l * l + l + mm;
-                const T g = t * zoff[prev] * dinv[j - 1];
+                const T g = t * zoff[prev] * pr[j - 1];
                 C y = v[idx * vs];
                 y = cmk<C>(fma(g, yp.y, y.x), fma(-g, yp.x, y.y));
                 v[idx * vs] = y;
                 yp = y;
             }
-            C xn = cmk<C>(yp.x * dinv[n - 1], yp.y * dinv[n - 1]);
+            C xn = cmk<C>(yp.x * pr[n - 1], yp.y * pr[n - 1]);
             v[idx * vs] = xn;
             for (int j = n - 2; j >= 0; --j) {
                 const int l = m + j;
                 idx = l * l + l + mm;
                 const T e = t * zoff[idx];
                 const C y = v[idx * vs];
-                xn = cmk<C>(fma(e, xn.y, y.x) * dinv[j], fma(-e, xn.x, y.y) * dinv[j]);
+                xn = cmk<C>(fma(e, xn.y, y.x) * pr[j], fma(-e, xn.x, y.y) * pr[j]);
                 v[idx * vs] = xn;
             }
         }
