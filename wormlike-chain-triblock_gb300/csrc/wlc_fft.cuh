@@ -206,6 +206,26 @@ template <int DIR, typename C> __device__ __forceinline__ C twid(const C* tw, in
     return w;
 }
 
+// Work items (line b, sub-transform j) of one sub-pass are dealt to the
+// threads line-fastest, j = w / nlines, b = w % nlines, stepped without a
+// division.  Lanes of a warp then touch different lines at the same element
+// offset: consecutive words for interleaved lines (lstride 1), and distinct
+// banks for contiguous lines when lstride is odd.
+struct LineWalk {
+    int b, j, sb, sj, nl;
+    __device__ __forceinline__ explicit LineWalk(int nlines)
+        : b((int)threadIdx.x % nlines), j((int)threadIdx.x / nlines), sb((int)blockDim.x % nlines),
+          sj((int)blockDim.x / nlines), nl(nlines) {}
+    __device__ __forceinline__ void next() {
+        b += sb;
+        j += sj;
+        if (b >= nl) {
+            b -= nl;
+            ++j;
+        }
+    }
+};
+
 // Batched in-place line FFTs: line b, element e at data[b*lstride + e*estride].
 template <int N, int DIR, typename C>
 __device__ __forceinline__ void fft_nat2perm(C* data, int nlines, int estride, int lstride, const C* tw) {
@@ -222,9 +242,9 @@ __device__ __forceinline__ void fft_nat2perm(C* data, int nlines, int estride, i
         }
         __syncthreads();
     } else {
-    for (int w = threadIdx.x; w < nlines * N2; w += blockDim.x) {
-        const int b = w / N2, j2 = w % N2;
-        C* ln = data + (size_t)b * lstride;
+    for (LineWalk it(nlines); it.j < N2; it.next()) {
+        const int j2 = it.j;
+        C* ln = data + (size_t)it.b * lstride;
         C v[N1];
 #pragma unroll
         for (int n1 = 0; n1 < N1; ++n1) v[n1] = ln[(n1 * N2 + j2) * estride];
@@ -237,9 +257,9 @@ __device__ __forceinline__ void fft_nat2perm(C* data, int nlines, int estride, i
         }
     }
     __syncthreads();
-    for (int w = threadIdx.x; w < nlines * N1; w += blockDim.x) {
-        const int b = w / N1, k1 = w % N1;
-        C* ln = data + (size_t)b * lstride;
+    for (LineWalk it(nlines); it.j < N1; it.next()) {
+        const int k1 = it.j;
+        C* ln = data + (size_t)it.b * lstride;
         C v[N2];
 #pragma unroll
         for (int n2 = 0; n2 < N2; ++n2) v[n2] = ln[(k1 * N2 + n2) * estride];
@@ -257,9 +277,9 @@ __device__ __forceinline__ void fft_perm2nat(C* data, int nlines, int estride, i
     if constexpr (N2 == 1) {
         fft_nat2perm<N, DIR>(data, nlines, estride, lstride, tw);
     } else {
-    for (int w = threadIdx.x; w < nlines * N1; w += blockDim.x) {
-        const int b = w / N1, k1 = w % N1;
-        C* ln = data + (size_t)b * lstride;
+    for (LineWalk it(nlines); it.j < N1; it.next()) {
+        const int k1 = it.j;
+        C* ln = data + (size_t)it.b * lstride;
         C v[N2];
 #pragma unroll
         for (int k2 = 0; k2 < N2; ++k2) v[k2] = ln[(k1 * N2 + k2) * estride];
@@ -272,9 +292,9 @@ __device__ __forceinline__ void fft_perm2nat(C* data, int nlines, int estride, i
         }
     }
     __syncthreads();
-    for (int w = threadIdx.x; w < nlines * N2; w += blockDim.x) {
-        const int b = w / N2, n2 = w % N2;
-        C* ln = data + (size_t)b * lstride;
+    for (LineWalk it(nlines); it.j < N2; it.next()) {
+        const int n2 = it.j;
+        C* ln = data + (size_t)it.b * lstride;
         C v[N1];
 #pragma unroll
         for (int k1 = 0; k1 < N1; ++k1) v[k1] = ln[(k1 * N2 + n2) * estride];

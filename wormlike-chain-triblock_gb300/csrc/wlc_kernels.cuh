@@ -15,11 +15,19 @@
 
 namespace wlc {
 
+// Element stride of one packed x row in the shared buffers of passes A and
+// C: N + 1 (odd), so that the line-fastest x-FFT work split puts the lanes
+// of a warp on distinct banks.  (N/2) rows of a plane then take
+// (N/2)(N+1) elements, an even count for the supported N (multiples of 4),
+// which keeps the buffers after them 16-byte aligned.
+__host__ __device__ constexpr int xrow(int N) { return N + 1; }
+__host__ __device__ constexpr int xplane(int N) { return (N / 2) * xrow(N); }
+
 // z planes per CTA of passes A and C: 32-byte runs per (col, i) in phat,
 // fewer when the half-spectrum planes would not fit in shared memory
 __host__ __device__ constexpr int zg_planes(int N, int tsize) {
     int z = 32 / (2 * tsize);
-    while (z > 1 && (size_t)(N + (N / 2) * N + z * N * (N / 2 + 1)) * 2 * tsize > 200 * 1024) z /= 2;
+    while (z > 1 && (size_t)(N + xplane(N) + z * N * (N / 2 + 1)) * 2 * tsize > 200 * 1024) z /= 2;
     return z;
 }
 

@@ -214,9 +214,9 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
     const int kyi = colid / a.nkx, kxi = colid % a.nkx;
     const int ix = fold_n(kxi, N), iy = fold_n(kyi, N);
     const double kx = ix * a.kf[0], ky = iy * a.kf[1];
-    const double rho = sqrt(kx * kx + ky * ky);
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
     if (threadIdx.x == 0) {
+        const double rho = sqrt(kx * kx + ky * ky);
         const double ca = rho > 0 ? kx / rho : 1.0, sa = rho > 0 ? ky / rho : 0.0;
         double cm = 1.0, sm2 = 0.0;
         for (int m = 0; m <= L; ++m) {
@@ -268,16 +268,37 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
     const T c0 = (T)a.c0, dcoef = (T)a.dcoef;
     const int iz = fold_n(perm_index<N>(p), N);
     const double kz = iz * a.kf[2];
-    const double kn = sqrt(rho * rho + kz * kz);
-    const double cb = kn > 0 ? kz / kn : 1.0, sb = kn > 0 ? rho / kn : 0.0;
-    const T t = (T)(a.sigma * a.ds * kn);
-    const T* pivrow = a.pivtab ? a.pivtab + (size_t)(ix * ix + iy * iy + iz * iz) * a.npiv : nullptr;
+    // angle of k to z and sigma ds |k|: in FP64 for FP64 propagators, in FP32
+    // for FP32 ones (every thread runs this, and the FP64 pipe is a small
+    // fraction of the FP32 pipe)
+    const int key = ix * ix + iy * iy + iz * iz;
+    const T* pivrow = a.pivtab ? a.pivtab + (size_t)key * a.npiv : nullptr;
+    T cb, sb, t;
+    if constexpr (sizeof(T) == 8) {
+        const double rho = sqrt(kx * kx + ky * ky);
+        const double kn = sqrt(rho * rho + kz * kz);
+        cb = kn > 0 ? kz / kn : 1.0;
+        sb = kn > 0 ? rho / kn : 0.0;
+        t = a.sigma * a.ds * kn;
+    } else {
+        // every operation rounded explicitly (no contraction choices, so all
+        // instantiations agree bit for bit); with a pivot table ds |k| is
+        // formed from the key exactly as the table forms it
+        const float kxf = __fmul_rn((float)ix, (float)a.kf[0]), kyf = __fmul_rn((float)iy, (float)a.kf[1]);
+        const float kzf = __fmul_rn((float)iz, (float)a.kf[2]);
+        const float rho = __fsqrt_rn(__fadd_rn(__fmul_rn(kxf, kxf), __fmul_rn(kyf, kyf)));
+        const float kn = __fsqrt_rn(__fadd_rn(__fmul_rn(rho, rho), __fmul_rn(kzf, kzf)));
+        cb = kn > 0.f ? __fdiv_rn(kzf, kn) : 1.f;
+        sb = kn > 0.f ? __fdiv_rn(rho, kn) : 0.f;
+        const float tk = pivrow ? __fmul_rn((float)(a.ds * a.kf[0]), __fsqrt_rn((float)key)) : __fmul_rn((float)a.ds, kn);
+        t = a.sigma > 0 ? tk : -tk;
+    }
     C* v = col + p;
-    rot_all<T>(v, NP, L, csa, (T)cb, (T)sb, 1, lmask);
+    rot_all<T>(v, NP, L, csa, cb, sb, 1, lmask);
     __syncthreads();
     tridiag_all<T>(v, NP, L, t, c0, dcoef, s_zoff, pivrow, mmask);
     __syncthreads();
-    rot_all<T>(v, NP, L, csa, (T)cb, (T)sb, 0, lmask);
+    rot_all<T>(v, NP, L, csa, cb, sb, 0, lmask);
     __syncthreads();
     if (correct) {
         // x -= G_cov^-1 (i sigma ds (k . dR) x), in FP32
@@ -327,7 +348,12 @@ __global__ void pivot_table(T* out, int nkeys, int L, double c0, double dcoef, d
                             const T* __restrict__ zoff) {
     const int npiv = (L + 1) * (L + 2) / 2;
     for (int key = blockIdx.x * blockDim.x + threadIdx.x; key < nkeys; key += gridDim.x * blockDim.x) {
-        const T t = (T)(ds * kf * sqrt((double)key));
+        // ds |k| as the solve kernel forms it for this precision
+        T t;
+        if constexpr (sizeof(T) == 8)
+            t = ds * kf * sqrt((double)key);
+        else
+            t = __fmul_rn((float)(ds * kf), __fsqrt_rn((float)key));
         T* row = out + (size_t)key * npiv;
         for (int m = 0; m <= L; ++m) {
             T* pr = row + m * (L + 1) - (m * (m - 1)) / 2;

@@ -91,20 +91,21 @@ template <int n> __device__ __forceinline__ void cp_async_wait() {
 // so that the Z values of one (col, i) run in phat move as one 32-byte chunk.
 
 // x-FFTs of ZB planes of packed row pairs (zb: ZB consecutive (N/2) x N
-// blocks), split into two half spectra each: planes zz0 .. zz0+ZB-1 of out
+// blocks, row stride xrow(N)), split into two half spectra each: planes zz0 .. zz0+ZB-1 of out
 // (the y-FFTs of all planes follow in one batched call, y_planes)
 template <typename T, int N, int Z, int ZB>
 __device__ __forceinline__ void fwd_x_planes(typename cvec<T>::t* zb, typename cvec<T>::t* out, int zz0,
                                              const typename cvec<T>::t* tw) {
     using C = typename cvec<T>::t;
     constexpr int NKX = N / 2 + 1;
-    fft_nat2perm<N, -1>(zb, ZB * (N / 2), 1, N, tw);
+    constexpr int XR = xrow(N);
+    fft_nat2perm<N, -1>(zb, ZB * (N / 2), 1, XR, tw);
     for (int t = threadIdx.x; t < ZB * (N / 2) * NKX; t += blockDim.x) {
         const int q = t / ((N / 2) * NKX), e = t % ((N / 2) * NKX);
         const int p = e / NKX, k = e % NKX;
-        const C* zq = zb + (size_t)q * (N / 2) * N;
-        const C zk = zq[p * N + perm_pos<N>(k)];
-        const C zm = zq[p * N + perm_pos<N>((N - k) % N)];
+        const C* zq = zb + (size_t)q * xplane(N);
+        const C zk = zq[p * XR + perm_pos<N>(k)];
+        const C zm = zq[p * XR + perm_pos<N>((N - k) % N)];
         out[((2 * p) * NKX + k) * Z + zz0 + q] = cmk<C>((T)0.5 * (zk.x + zm.x), (T)0.5 * (zk.y - zm.y));
         out[((2 * p + 1) * NKX + k) * Z + zz0 + q] = cmk<C>((T)0.5 * (zk.y + zm.y), (T)0.5 * (zm.x - zk.x));
     }
@@ -148,28 +149,35 @@ __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs
     constexpr int Z = XyShape<T, N, V>::Z, ZB = XyShape<T, N, V>::ZB;
     constexpr int NR = N * N * N;
     constexpr int PB = (N / 2) * N;  // packed row pairs per plane
+    constexpr int XR = xrow(N), PBS = xplane(N);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
-    C* zb = tw + N;                  // ZB x (N/2) x N packed row pairs
-    C* out = zb + (size_t)ZB * PB;   // N x NKX x Z half spectra
+    C* zb = tw + N;                  // ZB x (N/2) x N packed row pairs (row stride XR)
+    C* out = zb + (size_t)ZB * PBS;  // N x NKX x Z half spectra
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
     for (int zz0 = 0; zz0 < Z; zz0 += ZB) {
         if constexpr (sizeof(T) == 4) {
             // four consecutive x per thread: 16-byte loads of the history, ds*w
-            // and Theta planes (N is a multiple of 4)
+            // and Theta planes (N is a multiple of 4).  The four shared stores
+            // go out in an order rotated by (t / 4) % 4, which spreads the
+            // lanes of a warp over all bank pairs.
             for (int t = threadIdx.x; t < ZB * PB / 4; t += blockDim.x) {
                 const int q = t / (PB / 4), e = 4 * (t % (PB / 4));
                 const int p = e / N, x = e % N;
                 const size_t ra = ((size_t)(z0 + zz0 + q) * N + 2 * p) * N + x, rb = ra + N;
                 const float4 va = rhs_f32x4(a, (size_t)i * NR + ra, ra);
                 const float4 vb = rhs_f32x4(a, (size_t)i * NR + rb, rb);
-                C* zq = zb + (size_t)q * PB + e;
-                zq[0] = cmk<C>(va.x, vb.x);
-                zq[1] = cmk<C>(va.y, vb.y);
-                zq[2] = cmk<C>(va.z, vb.z);
-                zq[3] = cmk<C>(va.w, vb.w);
+                C* zq = zb + (size_t)q * PBS + p * XR + x;
+                const int rot = (t >> 2) & 3;
+#pragma unroll
+                for (int s = 0; s < 4; ++s) {
+                    const int c = (s + rot) & 3;
+                    const float xa = c == 0 ? va.x : c == 1 ? va.y : c == 2 ? va.z : va.w;
+                    const float xb = c == 0 ? vb.x : c == 1 ? vb.y : c == 2 ? vb.z : vb.w;
+                    zq[c] = cmk<C>(xa, xb);
+                }
             }
         } else {
             for (int t = threadIdx.x; t < ZB * PB; t += blockDim.x) {
@@ -178,7 +186,7 @@ __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs
                 const size_t ra = ((size_t)(z0 + zz0 + q) * N + 2 * p) * N + x, rb = ra + N;
                 const T va = rhs_value<T, NR>(a, (size_t)i * NR + ra, ra);
                 const T vb = rhs_value<T, NR>(a, (size_t)i * NR + rb, rb);
-                zb[(size_t)q * PB + e] = cmk<C>(va, vb);
+                zb[(size_t)q * PBS + p * XR + x] = cmk<C>(va, vb);
             }
         }
         __syncthreads();
@@ -193,7 +201,7 @@ __global__ void __launch_bounds__(512) rhs_fft_xy(StepArgs<T> a0, const StepArgs
 template <int N> struct StagedA {
     static constexpr int Z = zg_planes(N, 4);
     static constexpr size_t P = (size_t)N * N;
-    static constexpr size_t bytes = 8 * ((size_t)N + (N / 2) * (size_t)N + (size_t)Z * N * (N / 2 + 1)) + 2 * 4 * P * 4;
+    static constexpr size_t bytes = 8 * ((size_t)N + (size_t)xplane(N) + (size_t)Z * N * (N / 2 + 1)) + 2 * 4 * P * 4;
     static constexpr bool fits = bytes <= 220 * 1024;
 };
 
@@ -215,8 +223,8 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
     constexpr size_t P = StagedA<N>::P;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
-    C* zb = tw + N;
-    C* out = zb + (N / 2) * N;
+    C* zb = tw + N;                   // packed row pairs, row stride xrow(N)
+    C* out = zb + xplane(N);
     float* stage = reinterpret_cast<float*>(out + (size_t)Z * N * NKX);  // [2][4][P]
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
@@ -257,7 +265,7 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
                 va += a.msterm[(size_t)i * NR + zoff + ia];
                 vb += a.msterm[(size_t)i * NR + zoff + ib];
             }
-            zb[e] = make_float2(va, vb);
+            zb[p * xrow(N) + x] = make_float2(va, vb);
         }
         __syncthreads();
         fwd_x_planes<float, N, Z, 1>(zb, out, zz, tw);
@@ -275,10 +283,12 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
     constexpr int NKX = N / 2 + 1;
     constexpr int NR = N * N * N;
     constexpr int PB = (N / 2) * N;
+    constexpr int XR = xrow(N), PBS = xplane(N);
+    static_assert(PBS % 2 == 0, "the half-spectrum buffer must stay 16-byte aligned");
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* tw = reinterpret_cast<C*>(smem_raw);
-    C* zb = tw + N;
-    C* out = zb + (size_t)ZB * PB;
+    C* zb = tw + N;                   // packed row pairs, row stride XR
+    C* out = zb + (size_t)ZB * PBS;
     const int i = blockIdx.y;
     const int z0 = blockIdx.x * Z;
     for (int e = threadIdx.x; e < N; e += blockDim.x) tw[e] = a.twg[e];
@@ -318,14 +328,14 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
                 xa.y = -xa.y;
                 xb.y = -xb.y;
             }
-            zb[t] = cmk<C>(xa.x - xb.y, xa.y + xb.x);
+            zb[(size_t)q * PBS + p * XR + k] = cmk<C>(xa.x - xb.y, xa.y + xb.x);
         }
         __syncthreads();
-        fft_nat2perm<N, +1>(zb, ZB * (N / 2), 1, N, tw);  // along x; x at perm_pos(x)
+        fft_nat2perm<N, +1>(zb, ZB * (N / 2), 1, XR, tw);  // along x; x at perm_pos(x)
         for (int t = threadIdx.x; t < ZB * N * N; t += blockDim.x) {
             const int q = t / (N * N), e = t % (N * N);
             const int y = e / N, x = e % N;
-            const C v = zb[(size_t)q * PB + (y >> 1) * N + perm_pos<N>(x)];
+            const C v = zb[(size_t)q * PBS + (y >> 1) * XR + perm_pos<N>(x)];
             a.qout[(size_t)i * NR + (size_t)(z0 + zz0 + q) * N * N + e] = ((y & 1) ? v.y : v.x) * a.minv;
         }
         __syncthreads();
@@ -345,7 +355,7 @@ __global__ void __launch_bounds__(256) rhs_only(StepArgs<T> a, T* out) {
 template <typename T> size_t smem_xy(int N, int variant) {
     using C = typename cvec<T>::t;
     const int z = xy_planes(N, sizeof(T), variant & 1), zb = (variant & 2) ? z : 1;
-    return sizeof(C) * ((size_t)N + (size_t)zb * (N / 2) * N + (size_t)z * N * (N / 2 + 1));
+    return sizeof(C) * ((size_t)N + (size_t)zb * xplane(N) + (size_t)z * N * (N / 2 + 1));
 }
 
 template <typename T, int N, bool B> static void set_xy_attrs() {
