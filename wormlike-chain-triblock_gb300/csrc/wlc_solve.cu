@@ -41,32 +41,39 @@ __device__ __forceinline__ void dz_block(C* a, const T* cs, int sgn) {
     }
 }
 
-// D^T on block l: Xm Dz(-beta) Xp Dz(-alpha)
+// Dz(sgn * beta) on block a, with cos/sin(m beta) generated by the
+// recurrence from (cb, sb) = (cos beta, sin beta) as the block goes (no
+// table held in registers across blocks)
 template <int l, typename T, typename C>
-__device__ __forceinline__ void rot_in_block(C* v, int vs, const T* csa, const T* csb) {
-    constexpr int n = 2 * l + 1;
-    C a[n], b[n];
+__device__ __forceinline__ void dz_block_rec(C* a, T cb, T sb, int sgn) {
+    T cm = cb, sm = sb;
 #pragma unroll
-    for (int j = 0; j < n; ++j) a[j] = v[(l * l + j) * vs];
-    dz_block<l, T, C>(a, csa, -1);
-    XRot<l>::template p<T, C>(a, b);
-    dz_block<l, T, C>(b, csb, -1);
-    XRot<l>::template m<T, C>(b, a);
-#pragma unroll
-    for (int j = 0; j < n; ++j) v[(l * l + j) * vs] = a[j];
+    for (int m = 1; m <= l; ++m) {
+        const T s = sgn > 0 ? sm : -sm;
+        const C x = a[l + m], y = a[l - m];
+        a[l + m] = cmk<C>(cm * x.x - s * y.x, cm * x.y - s * y.y);
+        a[l - m] = cmk<C>(s * x.x + cm * y.x, s * x.y + cm * y.y);
+        const T cn = cm * cb - sm * sb, sn = sm * cb + cm * sb;
+        cm = cn;
+        sm = sn;
+    }
 }
 
-// D on block l: Dz(alpha) Xm Dz(beta) Xp
+// Block l of D^T (in = 1: Xm Dz(-beta) Xp Dz(-alpha)) or of D (in = 0:
+// Dz(alpha) Xm Dz(beta) Xp).  Both directions share one copy of the Xp and
+// Xm codelets (half the code of separate forward / backward bodies, which
+// keeps the instruction working set of the solve small).
 template <int l, typename T, typename C>
-__device__ __forceinline__ void rot_out_block(C* v, int vs, const T* csa, const T* csb) {
+__device__ __forceinline__ void rot_block(C* v, int vs, const T* csa, T cb, T sb, int in) {
     constexpr int n = 2 * l + 1;
     C a[n], b[n];
 #pragma unroll
     for (int j = 0; j < n; ++j) a[j] = v[(l * l + j) * vs];
+    if (in) dz_block<l, T, C>(a, csa, -1);
     XRot<l>::template p<T, C>(a, b);
-    dz_block<l, T, C>(b, csb, +1);
+    dz_block_rec<l, T, C>(b, cb, sb, in ? -1 : +1);
     XRot<l>::template m<T, C>(b, a);
-    dz_block<l, T, C>(a, csa, +1);
+    if (!in) dz_block<l, T, C>(a, csa, +1);
 #pragma unroll
     for (int j = 0; j < n; ++j) v[(l * l + j) * vs] = a[j];
 }
@@ -77,28 +84,13 @@ template <typename T>
 __device__ __noinline__ void rot_all(typename cvec<T>::t* v, int vs, int L, const T* csa, T cb, T sb, int in,
                                      unsigned lmask) {
     using C = typename cvec<T>::t;
-    T csb[2 * (kRotLmax + 1)];
-    {
-        T cm = (T)1, sm2 = (T)0;
-#pragma unroll
-        for (int m = 0; m <= kRotLmax; ++m) {
-            csb[2 * m] = cm;
-            csb[2 * m + 1] = sm2;
-            const T cn = cm * cb - sm2 * sb, sn = sm2 * cb + cm * sb;
-            cm = cn;
-            sm2 = sn;
-        }
-    }
 #pragma unroll 1
     for (int l = 0; l <= L; ++l) {
         if (!((lmask >> l) & 1u)) continue;
         switch (l) {
-#define WLC_ROT(q)                                          \
-    case q:                                                 \
-        if (in)                                             \
-            rot_in_block<q, T, C>(v, vs, csa, csb);         \
-        else                                                \
-            rot_out_block<q, T, C>(v, vs, csa, csb);        \
+#define WLC_ROT(q)                                      \
+    case q:                                             \
+        rot_block<q, T, C>(v, vs, csa, cb, sb, in);     \
         break;
             WLC_ROT(0) WLC_ROT(1) WLC_ROT(2) WLC_ROT(3) WLC_ROT(4) WLC_ROT(5) WLC_ROT(6)
             WLC_ROT(7) WLC_ROT(8) WLC_ROT(9) WLC_ROT(10) WLC_ROT(11) WLC_ROT(12)
@@ -134,15 +126,12 @@ __device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, 
                 dinv[j] = (T)1 / d;
             }
         }
-        for (int sgn = 1; sgn >= -1; sgn -= 2) {
-            if (sgn < 0 && m == 0) break;
-            const int mm = sgn * m;
-            int idx = m * m + m + mm;
-            C yp = v[idx * vs];
+        if (m == 0) {
+            int idx = 0;
+            C yp = v[0];
             for (int j = 1; j < n; ++j) {
-                const int l = m + j;
                 const int prev = idx;
-                idx = l * l + l + mm;
+                idx = j * j + j;
                 const T g = t * zoff[prev] * pr[j - 1];
                 C y = v[idx * vs];
                 y = cmk<C>(fma(g, yp.y, y.x), fma(-g, yp.x, y.y));
@@ -152,13 +141,46 @@ __device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, 
             C xn = cmk<C>(yp.x * pr[n - 1], yp.y * pr[n - 1]);
             v[idx * vs] = xn;
             for (int j = n - 2; j >= 0; --j) {
-                const int l = m + j;
-                idx = l * l + l + mm;
+                idx = j * j + j;
                 const T e = t * zoff[idx];
                 const C y = v[idx * vs];
                 xn = cmk<C>(fma(e, xn.y, y.x) * pr[j], fma(-e, xn.x, y.y) * pr[j]);
                 v[idx * vs] = xn;
             }
+            continue;
+        }
+        // the +m and -m systems share the pivots: both chains advance in
+        // lockstep (two independent dependency chains per step)
+        int ip = m * m + 2 * m, im = m * m;
+        C yp = v[ip * vs], ym = v[im * vs];
+        for (int j = 1; j < n; ++j) {
+            const int l = m + j;
+            const int pp = ip, pm = im;
+            ip = l * l + l + m;
+            im = l * l + l - m;
+            const T gp = t * zoff[pp] * pr[j - 1], gm = t * zoff[pm] * pr[j - 1];
+            C y1 = v[ip * vs], y2 = v[im * vs];
+            y1 = cmk<C>(fma(gp, yp.y, y1.x), fma(-gp, yp.x, y1.y));
+            y2 = cmk<C>(fma(gm, ym.y, y2.x), fma(-gm, ym.x, y2.y));
+            v[ip * vs] = y1;
+            v[im * vs] = y2;
+            yp = y1;
+            ym = y2;
+        }
+        C xp = cmk<C>(yp.x * pr[n - 1], yp.y * pr[n - 1]);
+        C xm = cmk<C>(ym.x * pr[n - 1], ym.y * pr[n - 1]);
+        v[ip * vs] = xp;
+        v[im * vs] = xm;
+        for (int j = n - 2; j >= 0; --j) {
+            const int l = m + j;
+            ip = l * l + l + m;
+            im = l * l + l - m;
+            const T ep = t * zoff[ip], em = t * zoff[im];
+            const C y1 = v[ip * vs], y2 = v[im * vs];
+            xp = cmk<C>(fma(ep, xp.y, y1.x) * pr[j], fma(-ep, xp.x, y1.y) * pr[j]);
+            xm = cmk<C>(fma(em, xm.y, y2.x) * pr[j], fma(-em, xm.x, y2.y) * pr[j]);
+            v[ip * vs] = xp;
+            v[im * vs] = xm;
         }
     }
 }

@@ -120,17 +120,25 @@ __device__ __forceinline__ void y_planes(typename cvec<T>::t* out, const typenam
     fft_nat2perm<N, DIR>(out, NKX * Z, NKX * Z, 1, tw);
 }
 
+// one Z-run per (ky, kx) from the half spectra to phat, in 16-byte pieces
+// when a run is a whole number of them (shared reads contiguous per lane)
 template <typename T, int N, int Z>
 __device__ __forceinline__ void store_phat(const StepArgs<T>& a, const typename cvec<T>::t* out, int i, int z0) {
     using C = typename cvec<T>::t;
     constexpr int NKX = N / 2 + 1;
+    constexpr int CH = (Z * (int)sizeof(C)) % 16 == 0 ? (Z * (int)sizeof(C)) / 16 : 0;
     for (int e = threadIdx.x; e < N * NKX; e += blockDim.x) {
         const int ky = e / NKX, kx = e % NKX;
         const size_t colid = (size_t)ky * NKX + kx;
         C* dst = a.phat + (colid * a.M + i) * N + z0;
         const C* src = out + (size_t)(perm_pos<N>(ky) * NKX + kx) * Z;
+        if constexpr (CH > 0) {
 #pragma unroll
-        for (int zz = 0; zz < Z; ++zz) dst[zz] = src[zz];
+            for (int q = 0; q < CH; ++q) reinterpret_cast<uint4*>(dst)[q] = reinterpret_cast<const uint4*>(src)[q];
+        } else {
+#pragma unroll
+            for (int zz = 0; zz < Z; ++zz) dst[zz] = src[zz];
+        }
     }
 }
 
@@ -332,11 +340,14 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
         }
         __syncthreads();
         fft_nat2perm<N, +1>(zb, ZB * (N / 2), 1, XR, tw);  // along x; x at perm_pos(x)
-        for (int t = threadIdx.x; t < ZB * N * N; t += blockDim.x) {
-            const int q = t / (N * N), e = t % (N * N);
-            const int y = e / N, x = e % N;
-            const C v = zb[(size_t)q * PBS + (y >> 1) * XR + perm_pos<N>(x)];
-            a.qout[(size_t)i * NR + (size_t)(z0 + zz0 + q) * N * N + e] = ((y & 1) ? v.y : v.x) * a.minv;
+        // packed row pair p holds rows 2p (real part) and 2p+1 (imaginary part)
+        for (int t = threadIdx.x; t < ZB * PB; t += blockDim.x) {
+            const int q = t / PB, e = t % PB;
+            const int p = e / N, x = e % N;
+            const C v = zb[(size_t)q * PBS + p * XR + perm_pos<N>(x)];
+            T* dst = a.qout + (size_t)i * NR + (size_t)(z0 + zz0 + q) * N * N + (size_t)(2 * p) * N + x;
+            dst[0] = v.x * a.minv;
+            dst[N] = v.y * a.minv;
         }
         __syncthreads();
     }
