@@ -81,8 +81,8 @@ __device__ __forceinline__ void rot_block(C* v, int vs, const T* csa, T cb, T sb
 // D^T (in = 1) or D (in = 0) on the degree blocks l set in lmask;
 // cos/sin(m beta) by recurrence from (cb, sb).  Compiled once per precision.
 template <typename T>
-__device__ __noinline__ void rot_all(typename cvec<T>::t* v, int vs, int L, const T* csa, T cb, T sb, int in,
-                                     unsigned lmask) {
+__device__ __noinline__ void rot_all(typename cvec<T>::t* __restrict__ v, int vs, int L, const T* __restrict__ csa, T cb,
+                                     T sb, int in, unsigned lmask) {
     using C = typename cvec<T>::t;
 #pragma unroll 1
     for (int l = 0; l <= L; ++l) {
@@ -105,8 +105,8 @@ __device__ __noinline__ void rot_all(typename cvec<T>::t* v, int vs, int L, cons
 // d_0 = A_m, d_j = A_l + e^2/d_{j-1}, e = t z_{l-1}; forward
 // y_l = b_l - i (e/d_{j-1}) y_{l-1}; back x_l = (y_l - i t z_l x_{l+1})/d_l.
 template <typename T>
-__device__ __noinline__ void tridiag_all(typename cvec<T>::t* v, int vs, int L, T t, T c0, T dcoef, const T* zoff,
-                                         const T* pivrow, unsigned mmask) {
+__device__ __noinline__ void tridiag_all(typename cvec<T>::t* __restrict__ v, int vs, int L, T t, T c0, T dcoef,
+                                         const T* __restrict__ zoff, const T* __restrict__ pivrow, unsigned mmask) {
     using C = typename cvec<T>::t;
 #pragma unroll 1
     for (int m = 0; m <= L; ++m) {
@@ -207,7 +207,8 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
     constexpr int NP = N + 1;
     const SolveTablesT<T>& g = a.tab;
     const int M = g.M, L = g.L;
-    const int correct = a.correct;
+    // the FP32 first-order correction exists in the FP64 path only
+    const int correct = sizeof(T) == 8 ? a.correct : 0;
     const SolveSmem sm = solve_smem(N, M, L, g.ndr, sizeof(T), correct);
     extern __shared__ __align__(16) unsigned char smem_raw[];
     C* col = reinterpret_cast<C*>(smem_raw + sm.col);

@@ -316,8 +316,10 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
     for (int zz0 = 0; zz0 < Z; zz0 += ZB) {
         // Hermitian extension of rows (2p, 2p+1) packed as one complex row;
         // the imaginary parts at kx = 0 and N/2 are discarded (c2r)
+        // plane index fastest across the lanes: the ZB values read per
+        // (row, k) are adjacent in out
         for (int t = threadIdx.x; t < ZB * PB; t += blockDim.x) {
-            const int q = t / PB, e = t % PB;
+            const int q = t % ZB, e = t / ZB;
             const int zz = zz0 + q;
             const int p = e / N, k = e % N;
             const C* ra = out + (size_t)perm_pos<N>(2 * p) * NKX * Z + zz;
