@@ -317,7 +317,7 @@ def run_ours(args, wl):
     roofline = {"bound": "hbm", "kernel": pass_names[dom], "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                 "bytes_per_launch": pb[dom], "avg_launch_ms": avg_ms, "kernel_share": share,
-                "binding_limit": ("FP64 pipe: 74-80 % active in every pass (ncu); the HBM fraction is"
+                "binding_limit": ("FP64 pipe: 75-84 % active in every pass (ncu); the HBM fraction is"
                                   " reported alongside") if bq == 8 else
                                  "latency-bound shared-memory FFT stages (ncu: 8-18 % DRAM, ~10 % FMA pipe)",
                 "step": {"algorithmic_bytes": b_step, "ms": step_ms,
