@@ -195,7 +195,11 @@ int wlc_mde_one_step(wlc_ctx* ctx, int32_t g_index, const double* pr, double* q_
  * needing more (M * (N/2+1) * N^2 * 16 bytes plus ~100 kB of tables) are
  * rejected with WLC_E_UNSUPPORTED.  The first call on a device looks up the
  * array's address and uploads the tables: make it before any stream
- * capture.  All calls share the array; calls that overlap on the GPU race.
+ * capture.  A call whose (N, L, literals) differs from the previous call's
+ * on that device uploads its own tables over the old ones and waits for the
+ * copy (WLC_E_STATE while its stream is being captured); work still queued
+ * on other streams then reads the new tables.  All calls share the array;
+ * calls that overlap on the GPU race.
  * stream: cudaStream_t or NULL; errbuf (may be NULL) receives a message. */
 int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, const double* pr_dev, double* q_out_dev,
                              void* stream, char* errbuf, int32_t errlen);

@@ -54,6 +54,102 @@ def test_single_precision_literals_deviate_at_float_rounding():
     assert 1e-9 < worst < 1e-7
 
 
+_W3J = {}
+
+
+def _w3j(l1, l2, l3, m1, m2, m3):
+    key = (l1, l2, l3, m1, m2, m3)
+    if key not in _W3J:
+        _W3J[key] = float(wigner_3j(l1, l2, l3, m1, m2, m3))
+    return _W3J[key]
+
+
+def test_three_j_matches_sympy_through_l12():
+    """Every 3j symbol the couplings use up to L = 12 (l3 = 1 for Rx/Ry/Rz,
+    l3 = 2 for Theta and J, and l3 = 0), across the FACTVALUE = 20 split of
+    (l1+l2+l3+1)! (SPH_mod.f90:104,116-122): l1+l2+l3+1 reaches 27."""
+    worst, split = 0.0, 0
+    for l1 in range(13):
+        for l3 in (0, 1, 2):
+            for l2 in range(max(0, l1 - l3), min(12, l1 + l3) + 1):
+                for m1 in range(-l1, l1 + 1):
+                    for m2 in range(-l2, l2 + 1):
+                        m3 = -m1 - m2
+                        if abs(m3) > l3:
+                            continue
+                        split += (l1 + l2 + l3 + 1) > 20
+                        worst = max(worst, abs(oracle.three_j(l1, l2, l3, m1, m2, m3) - _w3j(l1, l2, l3, m1, m2, m3)))
+    assert split > 1000  # the split path is exercised
+    assert worst < 1e-14
+
+
+def _real_sh_transform(l):
+    """Rows: real harmonics of degree l (m = -l..l) in terms of the complex
+    Y_l^mu, in the convention of sympy's real_gaunt (m < 0:
+    i/sqrt2 (Y^m - (-1)^m Y^-m); m > 0: 1/sqrt2 (Y^-m + (-1)^m Y^m))."""
+    u = np.zeros((2 * l + 1, 2 * l + 1), complex)
+    s = 1.0 / math.sqrt(2.0)
+    for m in range(-l, l + 1):
+        if m < 0:
+            u[m + l, m + l] = 1j * s
+            u[m + l, -m + l] = -1j * s * (-1) ** m
+        elif m == 0:
+            u[l, l] = 1.0
+        else:
+            u[m + l, -m + l] = s
+            u[m + l, m + l] = s * (-1) ** m
+    return u
+
+
+def _real_gaunt_exact(l1, l2, l3):
+    """Real Gaunt coefficients of one (l1, l2, l3) for all m, from sympy's
+    exact 3j symbols and the unitary map from complex to real harmonics."""
+    G = np.zeros((2 * l1 + 1, 2 * l2 + 1, 2 * l3 + 1), complex)
+    pre = math.sqrt((2 * l1 + 1) * (2 * l2 + 1) * (2 * l3 + 1) / (4 * math.pi)) * _w3j(l1, l2, l3, 0, 0, 0)
+    if pre != 0.0:
+        for a in range(-l1, l1 + 1):
+            for b in range(-l2, l2 + 1):
+                c = -a - b
+                if abs(c) <= l3:
+                    G[a + l1, b + l2, c + l3] = pre * _w3j(l1, l2, l3, a, b, c)
+    R = np.einsum("ia,jb,kc,abc->ijk", _real_sh_transform(l1), _real_sh_transform(l2), _real_sh_transform(l3), G)
+    assert np.abs(R.imag).max() < 1e-13
+    return R.real
+
+
+def test_exact_real_gaunt_restatement_matches_sympy():
+    """The 3j-based real Gaunt used below agrees with sympy's real_gaunt
+    (spot checks, including l = 12; real_gaunt itself is too slow for the
+    full sweep)."""
+    worst = 0.0
+    rng = np.random.default_rng(3)
+    for (l1, l2, l3) in [(2, 1, 1), (3, 3, 2), (12, 11, 1), (12, 12, 2), (10, 8, 2)]:
+        R = _real_gaunt_exact(l1, l2, l3)
+        for _ in range(3):
+            m1, m2 = int(rng.integers(-l1, l1 + 1)), int(rng.integers(-l2, l2 + 1))
+            for m3 in range(-l3, l3 + 1):
+                worst = max(worst, abs(R[m1 + l1, m2 + l2, m3 + l3] - float(real_gaunt(l1, l2, l3, m1, m2, m3))))
+    assert worst < 1e-15
+
+
+def test_triple_product_is_real_gaunt_through_l12():
+    """triple_product (double literals) equals sqrt(4 pi) times the real
+    Gaunt coefficient for every (l1, m1, l2, m2) up to L = 12 with l3 = 1
+    (Rx, Ry, Rz) and l3 = 2 (Theta, J) -- the whole coupling algebra of the
+    L = 8, 10, 12 workloads."""
+    worst, count = 0.0, 0
+    for l1 in range(13):
+        for l3 in (1, 2):
+            for l2 in range(max(0, l1 - l3), min(12, l1 + l3) + 1):
+                R = _real_gaunt_exact(l1, l2, l3) * math.sqrt(4 * math.pi)
+                for m1, m2, m3 in itertools.product(range(-l1, l1 + 1), range(-l2, l2 + 1), range(-l3, l3 + 1)):
+                    v = oracle.triple_product(l1, l2, l3, m1, m2, m3, 0)
+                    worst = max(worst, abs(v - R[m1 + l1, m2 + l2, m3 + l3]))
+                    count += 1
+    assert count > 80000
+    assert worst < 1e-14
+
+
 def _R(L, real4):
     o = oracle.Oracle((4, 4, 4), L, 6, (2, 2, 2), (0.1,) * 3, 1.0, (0.5,) * 3, (15,) * 3, real4=real4)
     return [o.matrix("RX"), o.matrix("RY"), o.matrix("RZ")], o

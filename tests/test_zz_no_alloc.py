@@ -54,6 +54,38 @@ def test_noalloc_matches_allocating_step_twice():
     inst.close()
 
 
+def test_noalloc_in_place_against_oracle_alternating_L():
+    """In place (q_out_dev == pr_dev, which the header allows) against the
+    CPU oracle, with (L, literals) changing between calls so that the
+    tables in the static array are replaced and then replaced back."""
+    import torch
+    import oracle
+    lib = wlc.load()
+    noalloc = _bind(lib)
+    n, nmax, ns = 12, 10, (4, 2, 4)
+    dx = 1.2 / n
+    kappa, chi = (0.5, 0.6, 0.7), (15.0, 15.0, 15.0)
+    rng = np.random.default_rng(77)
+    err = ctypes.create_string_buffer(256)
+    table = {3: (3, 1, 0), 5: (3, 1, 2), 8: (3, -1, 2)}
+    for L, lit, g_index in ((4, wlc.WLC_LIT_REAL4, 3), (6, wlc.WLC_LIT_REAL8, 8), (4, wlc.WLC_LIT_REAL4, 5)):
+        p = wlc.make_params(n, L, nmax, ns, dx, 1.3, kappa, chi, literals=lit)
+        o = oracle.Oracle((n, n, n), L, nmax, ns, (dx, dx, dx), 1.3, kappa, chi,
+                          real4=1 if lit == wlc.WLC_LIT_REAL4 else 0)
+        M = (L + 1) ** 2
+        pr = rng.standard_normal((M, n ** 3))
+        order, sigma, blk = table[g_index]
+        ref = o.one_step(order, sigma, blk, pr)
+        o.close()
+        d = torch.from_numpy(pr.copy()).cuda()
+        rc = noalloc(ctypes.byref(p), g_index, d.data_ptr(), d.data_ptr(), None, err, 256)
+        torch.cuda.synchronize()
+        assert rc == 0, err.value.decode()
+        out = d.cpu().numpy()
+        e = np.abs(out - ref).max() / np.abs(ref).max()
+        assert e < TOL, "L=%d G_index %d in place: rel err %.3e" % (L, g_index, e)
+
+
 def test_noalloc_rejects_sizes_above_static_limit():
     import torch
     lib = wlc.load()

@@ -315,7 +315,7 @@ int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
     *out = c;
     if (!build_basis_tables(c->L, c->real4, c->tab, why)) return set_err(c, WLC_E_SELFTEST, why);
     if ((rc = check_smem(c, c->fp32))) return rc;
-    prepare_reduce_kernels();
+    CK(prepare_reduce_kernels());
     if (ext) {
         c->st = ext;
         c->own_stream = false;

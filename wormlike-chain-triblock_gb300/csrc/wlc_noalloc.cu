@@ -15,9 +15,13 @@
 // device address (on the host it names a shadow symbol), so the first
 // call on each device, with that device current, looks up the real
 // address with cudaGetSymbolAddress and keeps it.  That first call also
-// copies the operator tables for (L, literal semantics) into the array;
-// make it before any stream capture.  Nothing here calls cudaMalloc,
-// cudaFree or an allocating library routine.
+// copies the operator tables for (N, L, literal semantics) into the array;
+// make it before any stream capture.  A later call with a different
+// (N, L, literals) copies that configuration's tables over them and waits
+// for the copy on its stream; while its stream is being captured such a
+// call is refused with WLC_E_STATE.  Work queued earlier on other streams
+// that still reads the array sees the new tables.  Nothing here calls
+// cudaMalloc, cudaFree or an allocating library routine.
 //
 // All calls share the one array: calls that overlap on the GPU (on
 // different streams, or from different host threads) race and corrupt
@@ -47,15 +51,22 @@ __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 struct DevState {
     bool ready = false;
     unsigned char* base = nullptr;  // device address of g_scratch
-    int L = -1, real4 = -1, N = -1;
+    int L = -1, real4 = -1, N = -1;  // configuration whose tables the array holds
     wlc::SolveTablesT<double> tab{};
     double2* twg = nullptr;
     double2* phat = nullptr;
 };
 
+// host-side tables of one (L, literal semantics) and the size of their
+// device image (which does not depend on the base address)
+struct HostTables {
+    wlc::BasisTables t;
+    size_t image_bytes = 0;
+};
+
 std::mutex g_mu;
 DevState g_dev[kMaxDevices];
-std::map<std::pair<int, int>, wlc::BasisTables> g_tables;  // host-side cache
+std::map<std::pair<int, int>, HostTables> g_tables;
 
 int fail(char* errbuf, int errlen, int code, const std::string& msg) {
     if (errbuf && errlen > 0) {
@@ -182,13 +193,13 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
     const auto key = std::make_pair(L, real4);
     auto it = g_tables.find(key);
     if (it == g_tables.end()) {
-        BasisTables t;
+        HostTables h;
         std::string why;
-        if (!build_basis_tables(L, real4, t, why)) return fail(errbuf, errlen, WLC_E_SELFTEST, why);
-        it = g_tables.emplace(key, std::move(t)).first;
+        if (!build_basis_tables(L, real4, h.t, why)) return fail(errbuf, errlen, WLC_E_SELFTEST, why);
+        h.image_bytes = make_image(h.t, ds.base).bytes.size();
+        it = g_tables.emplace(key, std::move(h)).first;
     }
-    TableImage im = make_image(it->second, ds.base);
-    const size_t tw_off = im.bytes.size();
+    const size_t tw_off = it->second.image_bytes;
     const size_t phat_off = align256(tw_off + sizeof(double2) * (size_t)N);
     const size_t need = phat_off + phat_bytes;
     if (need > kScratchBytes) {
@@ -200,7 +211,7 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
         return fail(errbuf, errlen, WLC_E_UNSUPPORTED, buf);
     }
     {
-        const BasisTables& t = it->second;
+        const BasisTables& t = it->second.t;
         const int ndr = (int)(t.dR[0].size() + t.dR[1].size() + t.dR[2].size());
         const size_t ssv =
             solve_smem(N, M, L, ndr, 8, ndr > 0 ? 1 : 0).total;
@@ -208,6 +219,17 @@ extern "C" int wlc_mde_one_step_noalloc(const wlc_params* p, int32_t g_index, co
             return fail(errbuf, errlen, WLC_E_UNSUPPORTED, "one coefficient column does not fit in shared memory");
     }
     if (ds.L != L || ds.real4 != real4 || ds.N != N) {
+        // (N, L, literals) changed since the last call on this device: the
+        // tables are re-uploaded, which blocks on the stream -- refused
+        // while the stream is being captured
+        cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+        if (cudaStreamIsCapturing(st, &cap) != cudaSuccess || cap != cudaStreamCaptureStatusNone) {
+            cudaGetLastError();
+            return fail(errbuf, errlen, WLC_E_STATE,
+                        "the operator tables of these (N, L, literals) must be uploaded outside stream capture: "
+                        "make one call with them before capturing");
+        }
+        const TableImage im = make_image(it->second.t, ds.base);
         std::vector<double2> tw(N);
         for (int j = 0; j < N; ++j) {
             const double a = 2.0 * M_PI * (double)j / (double)N;

@@ -10,6 +10,7 @@
 // tree in shared memory, one final CTA summing the partials in order.
 #include <cstdint>
 
+#include "wlc_attr.h"
 #include "wlc_reduce.h"
 
 namespace wlc {
@@ -583,19 +584,16 @@ WLC_INST(double)
 WLC_INST(float)
 #undef WLC_INST
 
-void prepare_reduce_kernels() {
-    static bool done = false;
-    if (done) return;
+cudaError_t prepare_reduce_kernels() {
+    // per (kernel, device): a context may be created on any device
     const int big = 200 * 1024;
-    cudaFuncSetAttribute(stensor_accum<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(stensor_accum<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(density_slice<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(density_slice<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(density_slice_batched<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(density_slice_batched<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(ms_term<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    cudaFuncSetAttribute(ms_term<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big);
-    done = true;
+    const void* fns[] = {(const void*)stensor_accum<double>, (const void*)stensor_accum<float>,
+                         (const void*)density_slice<double>, (const void*)density_slice<float>,
+                         (const void*)density_slice_batched<double>, (const void*)density_slice_batched<float>,
+                         (const void*)ms_term<double>, (const void*)ms_term<float>};
+    for (const void* fn : fns)
+        if (const cudaError_t e = smem_attr_once(fn, big); e != cudaSuccess) return e;
+    return cudaSuccess;
 }
 
 }  // namespace wlc

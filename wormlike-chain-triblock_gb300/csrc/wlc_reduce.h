@@ -53,9 +53,10 @@ struct JLists {
 template <typename T> struct PointTile {
     static constexpr int value = sizeof(T) == 8 ? 32 : 64;
 };
-// function attributes of the tiled kernels (large shared memory); call once
-// per process before any stream capture
-void prepare_reduce_kernels();
+// function attributes of the tiled kernels (large shared memory) on the
+// current device; call on each device before any stream capture (repeat
+// calls on a device return at once)
+cudaError_t prepare_reduce_kernels();
 constexpr int kMsGroups = 4;  // ms_term: row groups per point (threads per point)
 constexpr int kSGroups = 5;   // orientation tensor: one thread per component per point
 

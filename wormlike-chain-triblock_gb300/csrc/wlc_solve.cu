@@ -13,6 +13,7 @@
 // the grid spacing is isotropic.
 #include <cstdio>
 
+#include "wlc_attr.h"
 #include "wlc_kernels.cuh"
 #include "wlc_rot_gen.cuh"
 #include "wlc_step.h"
@@ -409,11 +410,7 @@ template <int N> static int solve_block(int threads) {
 }
 
 template <typename T, int N> static cudaError_t launch_solve_n(const SolveArgs<T>& a, cudaStream_t st, int threads) {
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaFuncSetAttribute(zfft_solve<T, N>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_done = true;
-    }
+    if (const cudaError_t e = smem_attr_once((const void*)zfft_solve<T, N>, 227 * 1024); e != cudaSuccess) return e;
     zfft_solve<T, N><<<a.nkx * N, solve_block<N>(threads), solve_smem_bytes<T>(a), st>>>(a, nullptr);
     return cudaGetLastError();
 }
@@ -431,18 +428,11 @@ template <typename T> cudaError_t launch_solve(int N, const SolveArgs<T>& a, cud
 }
 
 template <int N> static cudaError_t set_solve_batched_attr() {
-    static bool attr_done = false;
-    if (!attr_done) {
-        cudaError_t e =
-            cudaFuncSetAttribute(zfft_solve<float, N, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        if (e != cudaSuccess) return e;
-        attr_done = true;
-    }
-    return cudaSuccess;
+    return smem_attr_once((const void*)zfft_solve<float, N, true>, 227 * 1024);
 }
 
 template <int N> static cudaError_t launch_solve_batched_n(const BatchLaunch<float>& b, cudaStream_t st) {
-    set_solve_batched_attr<N>();
+    if (const cudaError_t e = set_solve_batched_attr<N>(); e != cudaSuccess) return e;
     zfft_solve<float, N, true><<<dim3(b.nkx * N, 1, b.count), solve_block<N>(b.solve_threads), b.solve_smem, st>>>(
         SolveArgs<float>{}, b.dsolve);
     return cudaGetLastError();

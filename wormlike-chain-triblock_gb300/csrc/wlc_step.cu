@@ -3,6 +3,7 @@
 // supported grid edge N and for FP64 / FP32.
 #include <cstdio>
 
+#include "wlc_attr.h"
 #include "wlc_kernels.cuh"
 #include "wlc_step.h"
 
@@ -371,25 +372,29 @@ template <typename T> size_t smem_xy(int N, int variant) {
     return sizeof(C) * ((size_t)N + (size_t)zb * xplane(N) + (size_t)z * N * (N / 2 + 1));
 }
 
-template <typename T, int N, bool B> static void set_xy_attrs() {
-    static bool done = false;
-    if (done) return;
-    cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(ifft_xy<T, N, B, 0>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    cudaFuncSetAttribute(ifft_xy<T, N, B, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-    if (smem_xy<T>(N, 2) <= 200 * 1024) {
-        cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(ifft_xy<T, N, B, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+// shared-memory limits of the pass A / pass C kernels of (T, N, B), once per
+// (kernel, device); returns the first error
+template <typename T, int N, bool B> static cudaError_t set_xy_attrs() {
+    constexpr int big = 200 * 1024;
+    cudaError_t e = cudaSuccess;
+    auto set = [&](const void* fn, int bytes) {
+        const cudaError_t r = smem_attr_once(fn, bytes);
+        if (e == cudaSuccess) e = r;
+    };
+    set((const void*)rhs_fft_xy<T, N, B, 0>, big);
+    set((const void*)ifft_xy<T, N, B, 0>, big);
+    set((const void*)rhs_fft_xy<T, N, B, 1>, big);
+    set((const void*)ifft_xy<T, N, B, 1>, big);
+    if (smem_xy<T>(N, 2) <= (size_t)big) {
+        set((const void*)rhs_fft_xy<T, N, B, 2>, big);
+        set((const void*)ifft_xy<T, N, B, 2>, big);
     }
-    if (smem_xy<T>(N, 3) <= 200 * 1024) {
-        cudaFuncSetAttribute(rhs_fft_xy<T, N, B, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaFuncSetAttribute(ifft_xy<T, N, B, 3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    if (smem_xy<T>(N, 3) <= (size_t)big) {
+        set((const void*)rhs_fft_xy<T, N, B, 3>, big);
+        set((const void*)ifft_xy<T, N, B, 3>, big);
     }
-    if constexpr (sizeof(T) == 4 && StagedA<N>::fits)
-        cudaFuncSetAttribute(rhs_fft_xy_staged<N, B>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)StagedA<N>::bytes);
-    done = true;
+    if constexpr (sizeof(T) == 4 && StagedA<N>::fits) set((const void*)rhs_fft_xy_staged<N, B>, (int)StagedA<N>::bytes);
+    return e;
 }
 
 // threads per CTA of the generic pass A and of pass C: 256 (default) or 512
@@ -431,7 +436,7 @@ static void launch_xy_any(int variant, bool do_a, const StepArgs<T>& a, const St
 
 template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s, cudaStream_t st) {
     constexpr int Z = zg_planes(N, sizeof(T));
-    set_xy_attrs<T, N, false>();
+    if (const cudaError_t ea = set_xy_attrs<T, N, false>(); ea != cudaSuccess) return ea;
     const dim3 gxy(N / Z, s.step.M);
     if (s.events) cudaEventRecord(s.events[0], st);
     if (s.do_a) {
@@ -452,7 +457,7 @@ template <typename T, int N> static cudaError_t launch_n(const StepLaunch<T>& s,
 
 template <int N> static cudaError_t launch_batched_n(const BatchLaunch<float>& b, cudaStream_t st) {
     constexpr int Z = zg_planes(N, 4);
-    set_xy_attrs<float, N, true>();
+    if (const cudaError_t ea = set_xy_attrs<float, N, true>(); ea != cudaSuccess) return ea;
     const dim3 gxy(N / Z, b.M, b.count);
     bool staged = false;
     if constexpr (StagedA<N>::fits) {
@@ -481,10 +486,11 @@ cudaError_t launch_step_batched(int N, const BatchLaunch<float>& b, cudaStream_t
 // function attributes of the batched kernels, set outside any stream capture
 cudaError_t prepare_step_batched(int N) {
     switch (N) {
-#define WLC_CASE(n)                          \
-    case n:                                  \
-        set_xy_attrs<float, n, true>();      \
-        return prepare_solve_batched(n);
+#define WLC_CASE(n)                                                       \
+    case n: {                                                             \
+        const cudaError_t ea = set_xy_attrs<float, n, true>();            \
+        return ea != cudaSuccess ? ea : prepare_solve_batched(n);         \
+    }
         WLC_FOR_EACH_BATCH_N(WLC_CASE)
 #undef WLC_CASE
         default:
