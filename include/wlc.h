@@ -51,6 +51,21 @@ enum { WLC_FP64 = 0, WLC_FP32 = 1 };
  * WLC_LIT_REAL8 = build with a default-real-8 promotion flag. */
 enum { WLC_LIT_REAL4 = 0, WLC_LIT_REAL8 = 1 };
 
+/* Contour-step scheme.
+ * WLC_SCHEME_BDF: the reference's semi-implicit BDF1/2/3 step with the
+ *   per-k solve of G(k) (mde_one_step / init_pr, MDE_ABC.f90:90-383) -- the
+ *   drop-in.
+ * WLC_SCHEME_SPLIT: no counterpart in the reference's harmonic-basis
+ *   solver.  Operator split of each step,
+ *     q(s) = e^{-w ds/2} C2R[ G_CN(k) R2C[ e^{-w ds/2} q(s-1) ] ] / N^3,
+ *     G_CN = (I + ds/2 A)^-1 (I - ds/2 A), A = Loa l(l+1)/(2 kappa) + i sigma k.R
+ *   (Strang splitting of the field term around a Crank-Nicolson step;
+ *   second order in ds, one history slice per step).  The field half steps
+ *   follow the reference's angular-grid split-operator solver
+ *   (split_operator_MDE_mod.f90:163-166,290-420).  Needs nmu = 0; not in
+ *   batches; wlc_init_pr and wlc_mde_one_step keep the BDF meaning. */
+enum { WLC_SCHEME_BDF = 0, WLC_SCHEME_SPLIT = 1 };
+
 /* Parameters of one ABC triblock instance: the union of input.txt
  * (initialize_mod.f90:59-84) and the reference's compile-time constants
  * (global_parameters.f90:32,52-60), with one L for all blocks. */
@@ -74,7 +89,8 @@ typedef struct wlc_params {
                            every K-th slice and recompute each segment of q during
                            the backward sweep (needs store_qstar 0 or 2; K ~ sqrt(3 Nmax)
                            minimises memory, at one extra forward sweep)           */
-    int32_t reserved[4];
+    int32_t scheme;     /* WLC_SCHEME_BDF (drop-in) or WLC_SCHEME_SPLIT                 */
+    int32_t reserved[3];
 } wlc_params;
 
 typedef struct wlc_ctx wlc_ctx;

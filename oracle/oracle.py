@@ -70,6 +70,8 @@ def _load():
     lib.orc_fft_r2c.argtypes = [P, Dp, Dp]
     lib.orc_fft_c2r.argtypes = [P, Dp, Dp]
     lib.orc_bench_step.argtypes = [P, Int, Dp]
+    lib.orc_set_scheme.argtypes = [P, Int]
+    lib.orc_split_step.argtypes = [P, Int, Int, Dp, Dp]
     lib.orc_three_j.argtypes = [Int] * 6
     lib.orc_three_j.restype = D
     lib.orc_triple_product.argtypes = [Int] * 7
@@ -93,7 +95,7 @@ def triple_product(l1, l2, l3, m1, m2, m3, real4=1):
 class Oracle:
     """One SCFT instance on the CPU (ABC triblock, one L for all blocks)."""
 
-    def __init__(self, n, L, nmax, ns, dx, loa, kappa, chi, nmu=0.0, real4=1, nthreads=None):
+    def __init__(self, n, L, nmax, ns, dx, loa, kappa, chi, nmu=0.0, real4=1, nthreads=None, scheme=0):
         lib = _load()
         self.lib = lib
         self.n = tuple(int(v) for v in n)
@@ -116,6 +118,8 @@ class Oracle:
                                 int(real4), self.nthreads)
         self.dx = tuple(float(v) for v in dx)
         self._loa = float(loa)
+        self.scheme = int(scheme)
+        lib.orc_set_scheme(self.h, self.scheme)
 
     def close(self):
         if self.h:
@@ -160,6 +164,13 @@ class Oracle:
         pr = np.ascontiguousarray(pr, dtype=np.float64).reshape(self.M, self.nr)
         out = np.empty((self.M, self.nr))
         self.lib.orc_one_step(self.h, int(order), int(sigma), int(blk), _dp(pr), _dp(out))
+        return out
+
+    def split_step(self, sigma, blk, q):
+        """One step of the operator-split scheme from slice q ([M][nr])."""
+        q = np.ascontiguousarray(q, dtype=np.float64).reshape(self.M, self.nr)
+        out = np.empty((self.M, self.nr))
+        self.lib.orc_split_step(self.h, int(sigma), int(blk), _dp(q), _dp(out))
         return out
 
     def propagate(self, direction):

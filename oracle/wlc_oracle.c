@@ -34,6 +34,18 @@
  *   free energy                            SCFT_Density_FE.f90:273-342 (AB form,
  *                                          generalised to three blocks)
  *
+ * Second contour-step scheme (scheme = 1, orc_set_scheme), which has no
+ * counterpart in the reference's harmonic-basis solver: the operator split
+ *   q(s) = e^{-w ds/2} C2R[ G_CN(k) R2C[ e^{-w ds/2} q(s-1) ] ] / N^3,
+ *   G_CN = (I + ds/2 A)^-1 (I - ds/2 A) = 2 (I + ds/2 A)^-1 - I,
+ *   A = Loa l(l+1)/(2 kappa) + i sigma (k.R),
+ * i.e. Strang splitting of the field term around a Crank-Nicolson step of
+ * the orientation and streaming terms.  Its real-space half steps follow the
+ * reference's angular-grid split-operator solver
+ * (split_operator_MDE_mod.f90:163-166,290-420); (I + ds/2 A) is the
+ * reference's G with c0 = 1 and ds/2.  Parity with the reference is
+ * unpinned for this scheme by construction.
+ *
  * Literal semantics.  The reference writes constants such as 11.0/6.0,
  * 1.0/3.0, 1.0/sqrt(3.0), sqrt(1.0*(2l1+1)...) and PI (declared REAL(SP)) as
  * default-kind reals, so a standard build evaluates them in single precision
@@ -314,7 +326,7 @@ static void fft1d(cplx* data, int stride, const fft_plan* p, int backward, cplx*
 #define ORC_MAXVAR 12
 
 typedef struct {
-    int order;    /* 1, 2, 3 */
+    int order;    /* 1, 2, 3 (BDF); 4: I + ds/2 A of the split scheme */
     double kappa; /* block kappa */
     cplx* lu;     /* [nk][M][M] LU factors of G(sigma=+1) */
     int* piv;     /* [nk][M] */
@@ -335,6 +347,7 @@ typedef struct {
     g_variant var[ORC_MAXVAR];
     int nvar;
     int nthreads;
+    int scheme; /* 0: the reference's BDF steps; 1: the operator split */
 } orc_ctx;
 
 static double lit_c0(int order, int real4) { /* Gmatrix_2dcomp_mod.f90:307-317 */
@@ -458,18 +471,20 @@ static void build_G(const orc_ctx* c, int kk, int order, double kappa, cplx* G) 
     int M = c->M;
     double kx, ky, kz;
     k_components(c, kk, &kx, &ky, &kz);
-    double c0 = lit_c0(order, c->real4);
+    /* order 4: the split scheme's I + ds/2 A (c0 = 1, step ds/2) */
+    double c0 = order == 4 ? 1.0 : lit_c0(order, c->real4);
+    double dse = order == 4 ? 0.5 * c->ds : c->ds;
     const double *Rx = c->mats[ORC_RX], *Ry = c->mats[ORC_RY], *Rz = c->mats[ORC_RZ];
     for (int i = 0; i < M; ++i)
         for (int j = 0; j < M; ++j) {
             size_t o = (size_t)i * M + j;
-            double gi = 1.0 * c->ds * (Rx[o] * kx + Ry[o] * ky + Rz[o] * kz);
+            double gi = 1.0 * dse * (Rx[o] * kx + Ry[o] * ky + Rz[o] * kz);
             G[o] = 0.0 + I * gi;
         }
     for (int j = 0; j < M; ++j) {
         int l, m;
         basis_lm(j, &l, &m);
-        double gr = c0 + c->ds * c->loa * l * (l + 1) / (2.0 * kappa);
+        double gr = c0 + dse * c->loa * l * (l + 1) / (2.0 * kappa);
         G[(size_t)j * M + j] = gr + I * cimag(G[(size_t)j * M + j]);
     }
 }
@@ -685,6 +700,8 @@ void orc_one_step(orc_ctx* c, int order, int sigma, int blk, const double* pr, d
                 lu_solve(A, piv, M, b);
                 for (int i = 0; i < M; ++i) b[i] = conj(b[i]);
             }
+            if (order == 4) /* Crank-Nicolson: (2 (I + ds/2 A)^-1 - I) b */
+                for (int i = 0; i < M; ++i) b[i] = 2.0 * b[i] - P[(size_t)i * nk + kk];
             for (int i = 0; i < M; ++i) P[(size_t)i * nk + kk] = b[i];
         }
 #pragma omp for
@@ -696,6 +713,27 @@ void orc_one_step(orc_ctx* c, int order, int sigma, int blk, const double* pr, d
         free(work);
     }
     free(P);
+}
+
+void orc_set_scheme(orc_ctx* c, int scheme) { c->scheme = scheme; }
+
+/* One step of the split scheme (block blk, direction sigma) from slice qin
+ * to qout: e^{-w ds/2} . C2R[ G_CN . R2C[ e^{-w ds/2} qin ] ] / N^3.  The
+ * field half steps follow split_operator_MDE_mod.f90:163-166. */
+void orc_split_step(orc_ctx* c, int sigma, int blk, const double* qin, double* qout) {
+    int M = c->M;
+    size_t nr = c->nr, sl = (size_t)M * nr;
+    const double* wb = c->w + (size_t)blk * nr;
+    double* eh = (double*)malloc(sizeof(double) * nr);
+    double* pr = (double*)calloc(sl, sizeof(double));
+    for (size_t r = 0; r < nr; ++r) eh[r] = exp(-0.5 * c->ds * wb[r]);
+    for (int i = 0; i < M; ++i)
+        for (size_t r = 0; r < nr; ++r) pr[(size_t)i * nr + r] = eh[r] * qin[(size_t)i * nr + r];
+    orc_one_step(c, 4, sigma, blk, pr, qout);
+    for (int i = 0; i < M; ++i)
+        for (size_t r = 0; r < nr; ++r) qout[(size_t)i * nr + r] *= eh[r];
+    free(pr);
+    free(eh);
 }
 
 /* block containing the forward step s-1 -> s (MDE_ABC.f90:44-57) */
@@ -741,6 +779,10 @@ void orc_propagate(orc_ctx* c, int dir) {
         memset(c->qf, 0, sizeof(double) * sl);
         for (size_t r = 0; r < nr; ++r) c->qf[r] = 1.0; /* q(0) = delta_i0 */
         for (int s = 1; s <= c->nmax; ++s) {
+            if (c->scheme == 1) {
+                orc_split_step(c, +1, blk_fwd(c, s), c->qf + (size_t)(s - 1) * sl, c->qf + (size_t)s * sl);
+                continue;
+            }
             orc_init_pr(c, +1, s, pr);
             int order = s < 3 ? s : 3;
             orc_one_step(c, order, +1, blk_fwd(c, s), pr, c->qf + (size_t)s * sl);
@@ -750,6 +792,10 @@ void orc_propagate(orc_ctx* c, int dir) {
         memset(top, 0, sizeof(double) * sl);
         for (size_t r = 0; r < nr; ++r) top[r] = 1.0; /* q*(Nmax) = delta_i0 */
         for (int s = c->nmax - 1; s >= 0; --s) {
+            if (c->scheme == 1) {
+                orc_split_step(c, -1, blk_bwd(c, s), c->qb + (size_t)(s + 1) * sl, c->qb + (size_t)s * sl);
+                continue;
+            }
             orc_init_pr(c, -1, s, pr);
             int d = c->nmax - s;
             int order = d < 3 ? d : 3;

@@ -161,6 +161,14 @@ static int validate(const wlc_params* p, std::string& why) {
         why = "q_checkpoint must be 0 or in [3, nmax], and needs store_qstar 0 or 2";
         return WLC_E_PARAM;
     }
+    if (p->scheme != WLC_SCHEME_BDF && p->scheme != WLC_SCHEME_SPLIT) {
+        why = "scheme must be WLC_SCHEME_BDF or WLC_SCHEME_SPLIT";
+        return WLC_E_PARAM;
+    }
+    if (p->scheme == WLC_SCHEME_SPLIT && std::fabs(p->nmu) >= 1.0e-5) {
+        why = "the split scheme has no Maier-Saupe term (nmu must be 0)";
+        return WLC_E_UNSUPPORTED;
+    }
     return WLC_OK;
 }
 
@@ -185,6 +193,14 @@ template <typename T> static int build_pivots(wlc_ctx* c) {
             c->launches++;
             if (e != cudaSuccess) return set_err(c, WLC_E_CUDA, std::string("pivot table: ") + cudaGetErrorString(e));
         }
+    if (split_scheme(c))  // I + ds/2 A per block: c0 = 1 at half the step
+        for (int b = 0; b < 3; ++b) {
+            T* out = (T*)c->pivtab + ((size_t)(9 + b) * c->nkeys) * c->npiv;
+            const double dcoef = 0.5 * c->ds * c->p.loa / (2.0 * c->p.kappa[b]);
+            cudaError_t e = launch_pivot_table<T>(out, c->nkeys, c->L, 1.0, dcoef, 0.5 * c->ds, c->kf[0], zoff, c->st);
+            c->launches++;
+            if (e != cudaSuccess) return set_err(c, WLC_E_CUDA, std::string("pivot table: ") + cudaGetErrorString(e));
+        }
     c->have_piv = true;
     return WLC_OK;
 }
@@ -203,7 +219,7 @@ template <typename T> static int alloc_fields(wlc_ctx* c) {
     c->qb = pt;
     if ((rc = dalloc(c, &pc, sizeof(C) * (size_t)c->nk * c->M))) return rc;
     c->phat = pc;
-    if ((rc = dalloc(c, &pt, sizeof(T) * 12 * (size_t)c->nr))) return rc;  // cf[3][3][nr] + dsw[3][nr]
+    if ((rc = dalloc(c, &pt, sizeof(T) * 15 * (size_t)c->nr))) return rc;  // cf[3][3][nr] + dsw[3][nr] + ehalf[3][nr]
     c->cf = pt;
     if ((rc = dalloc(c, &pt, sizeof(T) * sl))) return rc;
     c->work = pt;
@@ -244,7 +260,7 @@ template <typename T> static int use_precision(wlc_ctx* c) {
         if ((rc = build_twiddles<T>(c))) return rc;
         ps.twg = c->twg;
         void* pv = nullptr;
-        if ((rc = dalloc(c, (unsigned char**)&pv, (size_t)9 * c->nkeys * c->npiv * sizeof(T)))) return rc;
+        if ((rc = dalloc(c, (unsigned char**)&pv, (size_t)pivot_tables(c) * c->nkeys * c->npiv * sizeof(T)))) return rc;
         ps.pivtab = pv;
         ps.built = true;
         ps.piv_gen = -1;
@@ -487,7 +503,7 @@ static int contour_step(wlc_ctx* c, StepKind k, const T* h1, const T* h2, const 
         c->launches++;
         L.step.msterm = (const T*)c->msterm;
     }
-    return run_step<T>(c, L, lit_c0(k.order, c->real4), slot);
+    return run_step<T>(c, L, step_c0(c, k.order), slot);
 }
 
 // recompute q over segment m (slices mK+1 .. min(mK+K-1, Nmax)) into the
@@ -504,11 +520,11 @@ template <typename T> static int recompute_segment(wlc_ctx* c, int m) {
                            c->st));
     }
     for (int s = base + 1; s <= top; ++s) {
-        const int order = s < 3 ? s : 3;
+        const StepKind k = fwd_kind(c, s);
+        const int nh = hist_slices(k.order);
         const int i = s - base + 2;
-        int rc = contour_step<T>(c, StepKind{order, 1, blk_fwd(c, s)}, qf_seg<T>(c, i - 1),
-                                 order >= 2 ? qf_seg<T>(c, i - 2) : nullptr, order >= 3 ? qf_seg<T>(c, i - 3) : nullptr,
-                                 qf_seg<T>(c, i), -1);
+        int rc = contour_step<T>(c, k, qf_seg<T>(c, i - 1), nh >= 2 ? qf_seg<T>(c, i - 2) : nullptr,
+                                 nh >= 3 ? qf_seg<T>(c, i - 3) : nullptr, qf_seg<T>(c, i), -1);
         if (rc) return rc;
     }
     return WLC_OK;
@@ -530,9 +546,10 @@ template <typename T> static int sweep(wlc_ctx* c, int dir) {
         launch_set_delta<T>(at(0), c->M, c->nr, c->st);  // q(0) = delta_i0
         c->launches++;
         for (int s = 1; s <= nmax; ++s) {
-            const int order = s < 3 ? s : 3;
-            if ((rc = contour_step<T>(c, StepKind{order, 1, blk_fwd(c, s)}, at(s - 1), order >= 2 ? at(s - 2) : nullptr,
-                                      order >= 3 ? at(s - 3) : nullptr, at(s), s)))
+            const StepKind k = fwd_kind(c, s);
+            const int nh = hist_slices(k.order);
+            if ((rc = contour_step<T>(c, k, at(s - 1), nh >= 2 ? at(s - 2) : nullptr, nh >= 3 ? at(s - 3) : nullptr,
+                                      at(s), s)))
                 return rc;
             if (c->K) {
                 const int m = (s + 2) / c->K, j = s + 2 - m * c->K;
@@ -560,10 +577,10 @@ template <typename T> static int sweep(wlc_ctx* c, int dir) {
         slice(nmax);
         for (int n = 1; n <= nmax; ++n) {
             const int s = nmax - n;
-            const int order = n < 3 ? n : 3;
-            if ((rc = contour_step<T>(c, StepKind{order, -1, blk_bwd(c, s)}, qb_at<T>(c, s + 1),
-                                      order >= 2 ? qb_at<T>(c, s + 2) : nullptr,
-                                      order >= 3 ? qb_at<T>(c, s + 3) : nullptr, qb_at<T>(c, s), n)))
+            const StepKind k = bwd_kind(c, s);
+            const int nh = hist_slices(k.order);
+            if ((rc = contour_step<T>(c, k, qb_at<T>(c, s + 1), nh >= 2 ? qb_at<T>(c, s + 2) : nullptr,
+                                      nh >= 3 ? qb_at<T>(c, s + 3) : nullptr, qb_at<T>(c, s), n)))
                 return rc;
             if (c->K && (s + 1) % c->K == 0 && (rc = recompute_segment<T>(c, s / c->K))) return rc;
             slice(s);
@@ -788,6 +805,8 @@ extern "C" int wlc_init_pr(wlc_ctx* c, int32_t dir, int32_t s, double* pr) {
     if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must precede wlc_init_pr");
     if ((dir > 0 && c->K) || (dir < 0 && c->stream))
         return set_err(c, WLC_E_STATE, "that propagator is not stored (store_qstar / q_checkpoint)");
+    if (split_scheme(c))
+        return set_err(c, WLC_E_UNSUPPORTED, "wlc_init_pr is the BDF right-hand side; this context runs the split scheme");
     return c->fp32 ? init_pr_impl<float>(c, dir, s, pr) : init_pr_impl<double>(c, dir, s, pr);
 }
 
@@ -998,7 +1017,7 @@ template <typename T> static int autotune_impl(wlc_ctx* c) {
     const size_t sl = (size_t)c->M * c->nr;
     const int s = c->p.nmax;
     auto at = [&](int q) -> T* { return c->K ? qf_ring<T>(c, q) : (T*)c->qf + (size_t)q * sl; };
-    StepKind k{3, 1, blk_fwd(c, s)};
+    const StepKind k = fwd_kind(c, s);
     float best = 1e30f;
     int best_a = c->a_variant, best_t = c->solve_threads, best_x = c->xy_threads, best_z = c->xy_z;
     const bool ms = std::fabs(c->p.nmu) >= 1.0e-5 && c->have_mop;
@@ -1017,7 +1036,7 @@ template <typename T> static int autotune_impl(wlc_ctx* c) {
                                   c->M, c->nr, (T*)c->msterm, c->st);
                 L.step.msterm = (const T*)c->msterm;
             }
-            L.solve.c0 = lit_c0(3, c->real4);
+            L.solve.c0 = step_c0(c, k.order);
             const float ms_t = time_ms(c->st, [&] { launch_step<T>(c->N, L, c->st); }, 3);
             CK(cudaGetLastError());
             if (ms_t < best) {

@@ -253,10 +253,10 @@ extern "C" int wlc_batch_create(const wlc_params* p, int32_t count, wlc_batch** 
         const wlc_params& q = p[i];
         char buf[200];
         if (q.precision != WLC_FP32 || !supported_batch_n(q.n[0]) || q.q_checkpoint != 0 || q.nmax != p[0].nmax ||
-            q.lmax != p[0].lmax) {
+            q.lmax != p[0].lmax || q.scheme != WLC_SCHEME_BDF) {
             std::snprintf(buf, sizeof buf,
-                          "instance %d: batches take FP32 instances with one nmax and lmax, no q_checkpoint, and a "
-                          "grid edge in {16, 24, 32, 40, 48, 64}",
+                          "instance %d: batches take FP32 BDF-scheme instances with one nmax and lmax, no "
+                          "q_checkpoint, and a grid edge in {16, 24, 32, 40, 48, 64}",
                           i);
             return bset_err(b, WLC_E_UNSUPPORTED, buf);
         }

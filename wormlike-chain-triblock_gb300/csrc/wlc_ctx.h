@@ -146,6 +146,28 @@ inline int blk_bwd(const wlc_ctx* c, int s) {  // MDE_ABC.f90:69-83
     return 0;
 }
 
+inline bool split_scheme(const wlc_ctx* c) { return c->p.scheme == WLC_SCHEME_SPLIT; }
+// the step to slice s of the forward sweep / of the backward sweep: BDF order
+// ramp 1, 2, 3 at the chain ends (MDE_ABC.f90:50-56,70-82), or the split step
+inline StepKind fwd_kind(const wlc_ctx* c, int s) {
+    return StepKind{split_scheme(c) ? kSplitOrder : (s < 3 ? s : 3), 1, blk_fwd(c, s)};
+}
+inline StepKind bwd_kind(const wlc_ctx* c, int s) {
+    const int n = c->p.nmax - s;
+    return StepKind{split_scheme(c) ? kSplitOrder : (n < 3 ? n : 3), -1, blk_bwd(c, s)};
+}
+// diagonal constant of the solved operator: BDF c0, or 1 for I + ds/2 A
+inline double step_c0(const wlc_ctx* c, int order) {
+    return order == kSplitOrder ? 1.0 : lit_c0(order, c->real4);
+}
+// pivot tables per precision: (BDF order 1..3) x block, plus the split operator per block
+inline int pivot_tables(const wlc_ctx* c) { return split_scheme(c) ? 12 : 9; }
+// e^{-w_blk ds/2} plane of block blk in the coefficient array cf
+// ([blk][3][nr] BDF3 coefficients, [blk][nr] ds*w, [blk][nr] half-step factors)
+template <typename T> inline const T* ehalf_plane(const wlc_ctx* c, int blk) {
+    return (const T*)c->cf + (size_t)(12 + blk) * (size_t)c->nr;
+}
+
 // Fill the launch description of one step.  h1..h3: history (or the RHS
 // for order 0), qout: destination slice.
 template <typename T>
@@ -191,6 +213,19 @@ inline StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h
         s.pivtab = (const T*)c->pivtab + ((size_t)((k.order - 1) * 3 + k.blk) * c->nkeys) * c->npiv;
     // diagonal of G (Gmatrix_2dcomp_mod.f90:394): c0 + ds*Loa*l(l+1)/(2 kappa)
     s.dcoef = c->ds * c->p.loa / (2.0 * c->p.kappa[k.blk]);
+    if (k.order == kSplitOrder) {
+        // e^{-w ds/2} before and after; pass B solves I + ds/2 A (the G of
+        // c0 = 1 at half the step) and forms the Crank-Nicolson output
+        const T* eh = ehalf_plane<T>(c, k.blk);
+        a.cf = eh;
+        a.dsw = eh;
+        a.post = eh;
+        s.ds = 0.5 * c->ds;
+        s.dcoef = 0.5 * c->ds * c->p.loa / (2.0 * c->p.kappa[k.blk]);
+        s.split = 1;
+        if (c->have_piv)
+            s.pivtab = (const T*)c->pivtab + ((size_t)(9 + k.blk) * c->nkeys) * c->npiv;
+    }
     return L;
 }
 

@@ -38,6 +38,14 @@ __host__ __device__ constexpr int xy_planes(int N, int tsize, int zd) {
     return (zd == 1 && z / 2 >= 1 && ((z / 2) * 2 * tsize) % 16 == 0) ? z / 2 : z;
 }
 
+// StepArgs::order of a step of the operator-split scheme (WLC_SCHEME_SPLIT):
+// pass A multiplies q(s-1) by e^{-w ds/2} (cf / dsw hold that factor),
+// pass B applies the Crank-Nicolson operator, pass C multiplies by
+// e^{-w ds/2} again (post)
+constexpr int kSplitOrder = 4;
+// history slices read by a step of the given order (0: the given RHS)
+__host__ __device__ constexpr int hist_slices(int order) { return order == 2 ? 2 : order == 3 ? 3 : 1; }
+
 template <typename T> struct StepArgs {
     using C = typename cvec<T>::t;
     // pass A
@@ -45,11 +53,11 @@ template <typename T> struct StepArgs {
     const T* h2;
     const T* h3;
     const double* wb;   // block field [nr] (orders 1, 2)
-    const T* cf;        // order-3 coefficient planes [3][nr]
-    const T* dsw;       // ds * w of the block [nr] (FP32 staged path)
+    const T* cf;        // order-3 coefficient planes [3][nr]; split: e^{-w ds/2} [nr]
+    const T* dsw;       // ds * w of the block [nr] (FP32 path); split: e^{-w ds/2} [nr]
     T third;            // 1/3 of the BDF3 history (literal semantics)
     const T* msterm;    // optional ds*Theta*h term [M][nr] (Maier-Saupe) or null
-    int order;          // 0: h1 is the right-hand side itself; 1..3 BDF order
+    int order;          // 0: h1 is the right-hand side itself; 1..3 BDF order; kSplitOrder
     T ds;
     C* phat;            // [nkx*N][M][N]
     const C* twg;       // twiddle table exp(-2 pi i j/N), j < N
@@ -57,6 +65,7 @@ template <typename T> struct StepArgs {
     // pass C
     T* qout;            // [M][nr]
     T minv;             // 1/N^3
+    const T* post = nullptr;  // split scheme: e^{-w ds/2} [nr] applied after 1/N^3; null: none
 };
 
 // Per-context constant data of the factorised solve (device pointers).
@@ -99,6 +108,7 @@ template <typename T> struct SolveArgs {
     const T* pivtab;    // [key][npiv] inverse tridiagonal pivots of this
                         // (order, block), key = ix^2+iy^2+iz^2; null: on the fly
     int npiv;           // (L+1)(L+2)/2
+    int split = 0;      // 1: Crank-Nicolson output 2 G^-1 b - b (G = I + ds/2 A, ds here = half step)
 };
 
 // Shared-memory carve-up of the solve kernel (bytes, 16-aligned), shared by

@@ -61,7 +61,9 @@ template <typename T> __global__ void set_delta(T* q, int M, int64_t nr) {
 }
 
 // order-3 history coefficients per block: cf[blk][3][nr] =
-// (3 - 3 ds w, -3/2 + 3 ds w, third - ds w); then dsw[blk][nr] = ds w at cf + 9 nr
+// (3 - 3 ds w, -3/2 + 3 ds w, third - ds w); then dsw[blk][nr] = ds w at
+// cf + 9 nr and the split scheme's field half-step factors e^{-w ds/2} at
+// cf + 12 nr (split_operator_MDE_mod.f90:163-166)
 template <typename T>
 __global__ void make_cf(const double* __restrict__ w, T* __restrict__ cf, double ds, double third, int64_t nr) {
     for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < nr; r += (int64_t)gridDim.x * blockDim.x)
@@ -72,6 +74,7 @@ __global__ void make_cf(const double* __restrict__ w, T* __restrict__ cf, double
             o[nr + r] = (T)(-1.5 + 3.0 * ds * W);
             o[2 * nr + r] = (T)(third - ds * W);
             cf[(size_t)(9 + b) * nr + r] = (T)(ds * W);
+            cf[(size_t)(12 + b) * nr + r] = (T)exp(-0.5 * ds * W);
         }
 }
 

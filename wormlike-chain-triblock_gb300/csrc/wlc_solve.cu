@@ -362,7 +362,17 @@ __global__ void __launch_bounds__(kSolveThreads, (sizeof(T) == 4) ? 2 : 1)
     }
     __syncthreads();
     fft_perm2nat<N, +1>(col, M, 1, NP, tw);
-    for (int e = threadIdx.x; e < M * N; e += blockDim.x) gcol[e] = col[(e / N) * NP + (e % N)];
+    if (a.split) {
+        // Crank-Nicolson operator (I + ds/2 A)^-1 (I - ds/2 A) = 2 (I + ds/2 A)^-1 - I
+        // applied through the z transforms: IFFT_z(2x - b) = 2 IFFT_z(x) - N b,
+        // with b the column as pass A wrote it (still in phat)
+        for (int e = threadIdx.x; e < M * N; e += blockDim.x) {
+            const C x = col[(e / N) * NP + (e % N)], b = gcol[e];
+            gcol[e] = cmk<C>(fma((T)2, x.x, -(T)N * b.x), fma((T)2, x.y, -(T)N * b.y));
+        }
+    } else {
+        for (int e = threadIdx.x; e < M * N; e += blockDim.x) gcol[e] = col[(e / N) * NP + (e % N)];
+    }
 }
 
 // inverse pivots 1/d_j of the tridiagonal systems for every key

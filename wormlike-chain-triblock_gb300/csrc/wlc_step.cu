@@ -17,8 +17,10 @@ __device__ __forceinline__ int fold_idx(int i, int n) { return i <= n / 2 ? i : 
 // c = (3 - 3 ds w, -3/2 + 3 ds w, 1/3 - ds w) precomputed per block.
 // FP32 form shared by both pass-A kernels (so that they give identical
 // results): dw = ds w(r) rounded once, every operation rounded explicitly.
+// Split-scheme steps (kSplitOrder) pass e^{-w ds/2} as dw: q1 e^{-w ds/2}.
 __device__ __forceinline__ float rhs_f32(int order, float q1, float q2, float q3, float dw, float third) {
     if (order == 0) return q1;
+    if (order == kSplitOrder) return __fmul_rn(dw, q1);
     if (order == 1) return __fmul_rn(__fsub_rn(1.0f, dw), q1);
     if (order == 2) {
         const float t = __fsub_rn(__fmul_rn(2.0f, q1), q2);
@@ -33,14 +35,17 @@ template <typename T, int NR>
 __device__ __forceinline__ T rhs_value(const StepArgs<T>& a, size_t off, size_t r) {
     if constexpr (sizeof(T) == 4) {
         const int o = a.order;
-        float v = rhs_f32(o, a.h1[off], o >= 2 ? a.h2[off] : 0.0f, o >= 3 ? a.h3[off] : 0.0f, o >= 1 ? a.dsw[r] : 0.0f,
-                          a.third);
+        const int nh = hist_slices(o);
+        float v = rhs_f32(o, a.h1[off], nh >= 2 ? a.h2[off] : 0.0f, nh >= 3 ? a.h3[off] : 0.0f,
+                          o >= 1 ? a.dsw[r] : 0.0f, a.third);
         if (a.msterm) v += a.msterm[off];
         return v;
     }
     T v;
     if (a.order == 0) {
         v = a.h1[off];
+    } else if (a.order == kSplitOrder) {  // e^{-w ds/2} q(s-1)
+        v = a.cf[r] * a.h1[off];
     } else if (a.order == 1) {
         const T W = (T)a.wb[r];
         v = ((T)1 - a.ds * W) * a.h1[off];
@@ -61,10 +66,11 @@ __device__ __forceinline__ T rhs_value(const StepArgs<T>& a, size_t off, size_t 
 __device__ __forceinline__ float4 ld4(const float* p) { return *reinterpret_cast<const float4*>(p); }
 __device__ __forceinline__ float4 rhs_f32x4(const StepArgs<float>& a, size_t off, size_t r) {
     const int o = a.order;
+    const int nh = hist_slices(o);
     const float4 z4 = make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 q1 = ld4(a.h1 + off);
-    const float4 q2 = o >= 2 ? ld4(a.h2 + off) : z4;
-    const float4 q3 = o >= 3 ? ld4(a.h3 + off) : z4;
+    const float4 q2 = nh >= 2 ? ld4(a.h2 + off) : z4;
+    const float4 q3 = nh >= 3 ? ld4(a.h3 + off) : z4;
     const float4 dw = o >= 1 ? ld4(a.dsw + r) : z4;
     float4 v = make_float4(rhs_f32(o, q1.x, q2.x, q3.x, dw.x, a.third), rhs_f32(o, q1.y, q2.y, q3.y, dw.y, a.third),
                            rhs_f32(o, q1.z, q2.z, q3.z, dw.z, a.third), rhs_f32(o, q1.w, q2.w, q3.w, dw.w, a.third));
@@ -217,7 +223,7 @@ template <int N> struct StagedA {
 __device__ __forceinline__ float rhs_staged(const float* st, int order, size_t P, size_t idx, float third) {
     const float q1 = st[idx];
     if (order == 0) return q1;
-    if (order == 1) return rhs_f32(1, q1, 0.0f, 0.0f, st[P + idx], third);
+    if (order == 1 || order == kSplitOrder) return rhs_f32(order, q1, 0.0f, 0.0f, st[P + idx], third);
     if (order == 2) return rhs_f32(2, q1, st[P + idx], 0.0f, st[2 * P + idx], third);
     return rhs_f32(3, q1, st[P + idx], st[2 * P + idx], st[3 * P + idx], third);
 }
@@ -241,8 +247,8 @@ __global__ void __launch_bounds__(512) rhs_fft_xy_staged(StepArgs<float> a0, con
     const float* src[4];
     int ns = 0;
     src[ns++] = a.h1 + (size_t)i * NR;
-    if (order >= 2) src[ns++] = a.h2 + (size_t)i * NR;
-    if (order >= 3) src[ns++] = a.h3 + (size_t)i * NR;
+    if (hist_slices(order) >= 2) src[ns++] = a.h2 + (size_t)i * NR;
+    if (hist_slices(order) >= 3) src[ns++] = a.h3 + (size_t)i * NR;
     if (order >= 1) src[ns++] = a.dsw;
     auto issue = [&](int zz, int buf) {
         const size_t zoff = (size_t)(z0 + zz) * P;
@@ -348,9 +354,15 @@ __global__ void __launch_bounds__(512) ifft_xy(StepArgs<T> a0, const StepArgs<T>
             const int q = t / PB, e = t % PB;
             const int p = e / N, x = e % N;
             const C v = zb[(size_t)q * PBS + p * XR + perm_pos<N>(x)];
-            T* dst = a.qout + (size_t)i * NR + (size_t)(z0 + zz0 + q) * N * N + (size_t)(2 * p) * N + x;
-            dst[0] = v.x * a.minv;
-            dst[N] = v.y * a.minv;
+            const size_t r = (size_t)(z0 + zz0 + q) * N * N + (size_t)(2 * p) * N + x;
+            T* dst = a.qout + (size_t)i * NR + r;
+            if (a.post) {  // split scheme: the second field half step
+                dst[0] = (v.x * a.minv) * a.post[r];
+                dst[N] = (v.y * a.minv) * a.post[r + N];
+            } else {
+                dst[0] = v.x * a.minv;
+                dst[N] = v.y * a.minv;
+            }
         }
         __syncthreads();
     }

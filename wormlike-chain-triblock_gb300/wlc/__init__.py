@@ -27,6 +27,7 @@ _LIB = None
 
 WLC_FP64, WLC_FP32 = 0, 1
 WLC_LIT_REAL4, WLC_LIT_REAL8 = 0, 1
+WLC_SCHEME_BDF, WLC_SCHEME_SPLIT = 0, 1
 ERRORS = {-1: "WLC_E_PARAM", -2: "WLC_E_ALLOC", -3: "WLC_E_CUDA", -4: "WLC_E_STATE",
           -5: "WLC_E_NONFINITE", -6: "WLC_E_UNSUPPORTED", -7: "WLC_E_SELFTEST", -8: "WLC_E_IO"}
 
@@ -55,7 +56,8 @@ class Params(ctypes.Structure):
                 ("ns", ctypes.c_int32 * 3), ("dx", ctypes.c_double * 3), ("loa", ctypes.c_double),
                 ("kappa", ctypes.c_double * 3), ("chi", ctypes.c_double * 3), ("nmu", ctypes.c_double),
                 ("precision", ctypes.c_int32), ("literals", ctypes.c_int32),
-                ("store_qstar", ctypes.c_int32), ("q_checkpoint", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+                ("store_qstar", ctypes.c_int32), ("q_checkpoint", ctypes.c_int32), ("scheme", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 3)]
 
 
 class MixParams(ctypes.Structure):
@@ -187,7 +189,7 @@ def wlc_radius_of_gyration(x):
 
 
 def make_params(n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_FP64, literals=WLC_LIT_REAL4,
-                store_qstar=1, q_checkpoint=0):
+                store_qstar=1, q_checkpoint=0, scheme=WLC_SCHEME_BDF):
     """wlc_params of one instance (kappa, chi: 3-tuples; n, dx: scalar or 3-tuple)."""
     p = Params()
     n = (n, n, n) if np.isscalar(n) else tuple(n)
@@ -205,6 +207,7 @@ def make_params(n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_F
     p.literals = int(literals)
     p.store_qstar = int(store_qstar)
     p.q_checkpoint = int(q_checkpoint)
+    p.scheme = int(scheme)
     return p
 
 
@@ -212,9 +215,10 @@ class Instance:
     """One ABC-triblock instance on the current CUDA device."""
 
     def __init__(self, n, lmax, nmax, ns, dx, loa, kappa, chi, nmu=0.0, precision=WLC_FP64,
-                 literals=WLC_LIT_REAL4, store_qstar=1, q_checkpoint=0):
+                 literals=WLC_LIT_REAL4, store_qstar=1, q_checkpoint=0, scheme=WLC_SCHEME_BDF):
         self.lib = load()
-        p = make_params(n, lmax, nmax, ns, dx, loa, kappa, chi, nmu, precision, literals, store_qstar, q_checkpoint)
+        p = make_params(n, lmax, nmax, ns, dx, loa, kappa, chi, nmu, precision, literals, store_qstar, q_checkpoint,
+                        scheme)
         self._init_from(p)
         self.owned = True
         self.h = ctypes.c_void_p()
