@@ -71,6 +71,7 @@ def _load():
     lib.orc_fft_c2r.argtypes = [P, Dp, Dp]
     lib.orc_bench_step.argtypes = [P, Int, Dp]
     lib.orc_set_scheme.argtypes = [P, Int]
+    lib.orc_bench_steps.argtypes = [P, Int, Dp]
     lib.orc_split_step.argtypes = [P, Int, Int, Dp, Dp]
     lib.orc_three_j.argtypes = [Int] * 6
     lib.orc_three_j.restype = D
@@ -212,6 +213,13 @@ class Oracle:
         self.lib.orc_bench_step(self.h, int(nk_sample), _dp(t))
         est = t[0] + t[1] + t[2] * self.nk / max(1, min(nk_sample, self.nk)) + t[3]
         return t, est
+
+    def bench_steps(self, nsteps):
+        """Timed whole BDF3 contour steps (every wavevector, plus the slice's
+        density contribution); returns (set-up s, timed s, s per step)."""
+        t = np.zeros(3)
+        self.lib.orc_bench_steps(self.h, int(nsteps), _dp(t))
+        return float(t[0]), float(t[1]), float(t[2])
 
     def fft_r2c(self, a):
         a = np.ascontiguousarray(a, dtype=np.float64).reshape(self.nr)

@@ -1075,3 +1075,47 @@ void orc_bench_step(orc_ctx* c, int nk_sample, double* t) {
     free(lu);
     free(piv);
 }
+
+/* Timed sample of whole BDF3 contour steps (the CPU baseline of the
+ * contour-step throughput): `nsteps` forward steps of block A, each the
+ * right-hand side from the last three slices (init_pr, MDE_ABC.f90:245-309),
+ * the R2C FFTs, the per-k solve at EVERY wavevector, the C2R FFTs
+ * (mde_one_step, wormlike_MDE_2dcomp_mod.f90:357-455), and the slice's
+ * Simpson-weighted q . q* contribution to a block density accumulator
+ * (SCFT_Density_FE_ABC.f90:102-117).  The slices live in a ring of four
+ * (the context needs nmax >= 4); q* is the stored slice q_star(0).  The LU
+ * factors of G(k), which the reference precomputes once per box
+ * (init_inverse_sparse_GAB, Gmatrix_2dcomp_mod.f90:222-652), are built
+ * before the clock starts.  t[0]: set-up seconds (LU factors), t[1]: timed
+ * seconds for the nsteps steps, t[2]: seconds per step. */
+void orc_bench_steps(orc_ctx* c, int nsteps, double* t) {
+    int M = c->M;
+    size_t nr = c->nr, sl = (size_t)M * nr;
+    double ts = now_s();
+    get_variant(c, 3, c->kappa[0]);
+    double t0 = now_s();
+    double* pr = (double*)malloc(sizeof(double) * sl);
+    double* acc = (double*)calloc(nr, sizeof(double));
+    const double* qs = c->qb;
+    for (int s = 3; s < 3 + nsteps; ++s) {
+        double* q1 = c->qf + (size_t)((s - 1) & 3) * sl;
+        double* q2 = c->qf + (size_t)((s - 2) & 3) * sl;
+        double* q3 = c->qf + (size_t)((s - 3) & 3) * sl;
+        double* out = c->qf + (size_t)(s & 3) * sl;
+        rhs(c, 3, q1, q2, q3, c->w, pr);
+        orc_one_step(c, 3, +1, 0, pr, out);
+        const double wgt = (s & 1) ? 4.0 : 2.0; /* interior Simpson weights (times ds/3) */
+#pragma omp parallel for num_threads(c->nthreads)
+        for (long r = 0; r < (long)nr; ++r) {
+            double v = 0.0;
+            for (int i = 0; i < M; ++i) v += out[(size_t)i * nr + r] * qs[(size_t)i * nr + r];
+            acc[r] += wgt * c->ds / 3.0 * v;
+        }
+    }
+    double t1 = now_s();
+    t[0] = t0 - ts;
+    t[1] = t1 - t0;
+    t[2] = (t1 - t0) / (nsteps > 0 ? nsteps : 1);
+    free(pr);
+    free(acc);
+}
