@@ -451,99 +451,133 @@ def run_profile_case(args):
     inst.close()
 
 
-def run_converge(args):
-    """Time-to-converged F at the bench workload: the SCFT loop (propagators,
-    densities, free energy, field update on the device) from the same seeded
-    cold start until every block residual is <= tol, for each form:
-      fp64       plain FP64 propagators throughout (the drop-in);
-      fp32sched  FP32 propagators until the residual falls below
-                 --switch-tol, then FP64 to the end (same fields and
-                 mixing history);
-      fp32       FP32 propagators throughout (reports where FP32 stalls).
-    FP64 Q, F, residuals and the Anderson least squares in every form.
-    Wall time includes everything; capped by --budget seconds per form."""
+def c2_draw(seed):
+    """The headline instance as a warm-start draw (64^3 run, box 5.0 Rg)."""
+    return dict(fa=0.25, fc=0.25, chi=18.0, x=2.0, box=5.0, noise_seed=int(seed))
+
+
+def converge_form(wl, w0, form, args):
+    """One SCFT run to residual <= args.tol from fields w0 (wall time
+    includes everything: propagators, densities copied back, free energy,
+    field update on the device).  form 'fp64': FP64 propagators throughout;
+    'fp32': FP32 propagators until the residual falls below --switch-tol or
+    stops improving for --stall iterations (FP32's floor), then FP64 with a
+    fresh Anderson history (one simple-mixing iteration, then Anderson)."""
     import torch
     import wlc
-    wl = workload("fp64")
-    nr = wl["n"] ** 3
-    rng = np.random.default_rng(2024)
-    w0 = rng.normal(0.0, wl["w_sigma"], size=(3, nr))
-    if args.seed_kind == "lamellar":
-        # lamellar start: A and C stripes in antiphase along x, B between them,
-        # amplitude 1.0, plus seeded N(0, 0.1^2) noise
-        n = wl["n"]
-        x = (np.arange(nr) % n) / n
-        c1, c2 = np.cos(2 * np.pi * x), np.cos(4 * np.pi * x)
-        w0 = np.stack([c1, c2, -c1]) + rng.normal(0.0, 0.1, size=(3, nr))
-    if args.init_w:  # restart from saved fields (the reference's readW restart)
-        w0 = np.load(args.init_w)
+    prec = wlc.WLC_FP32 if form == "fp32" else wlc.WLC_FP64
+    inst = wlc.Instance(wl["n"], wl["L"], wl["nmax"], wl["ns"], wl["dx"], wl["loa"], wl["kappa"], wl["chi"],
+                        precision=prec, store_qstar=1 if args.stored else 0)
+    inst.set_fields(w0)
+    if not args.no_autotune:
+        inst.autotune()
     mp = wlc.mix_params(anderson_depth=args.depth, num_simple=20, lambda_anderson=args.lambda_a, tol=args.tol,
                         min_iter=20, relax_iter=0)
-    out = {"metric": "time-to-converged F (64^3, L=10, Ns=200, ABC; residual <= %g)" % args.tol,
-           "mixing": {"anderson_depth": args.depth, "num_simple": 20, "lambda_simple": 0.1,
-                      "lambda_anderson": args.lambda_a, "ramp": args.ramp}, "forms": {}}
-    for form in args.forms.split(","):
-        prec = wlc.WLC_FP64 if form == "fp64" else wlc.WLC_FP32
-        inst = wlc.Instance(wl["n"], wl["L"], wl["nmax"], wl["ns"], wl["dx"], wl["loa"], wl["kappa"], wl["chi"],
-                            precision=prec)
-        inst.set_fields(w0)
-        mp.lambda_anderson = args.lambda_a
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        hist, switched, n, conv = [], None, 0, False
-        t_switch = None
-        while not conv and n < args.max_iter and time.perf_counter() - t0 < args.budget:
-            if args.stop_at > 0 and hist and max(hist[-1][3:6]) < args.stop_at and n > 20:
-                break
-            n += 1
-            if args.ramp and n > 20:  # lambda_A = max(lambda_a, 1 - 0.9^(n - 20))
-                mp.lambda_anderson = max(args.lambda_a, 1.0 - 0.9 ** (n - 20))
-            inst.MDE_q()
-            inst.MDE_qstar()
-            d = inst.density(want_junction=False)
-            fe = inst.free_energy()
-            err, conv = inst.iterate(mp)
-            hist.append([n, fe, d["lnQ"]] + [float(e) for e in err])
-            if form == "fp32sched" and switched is None and max(err[:3]) < args.switch_tol and n > 20:
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    inst.set_fields(w0)
+    hist, n, conv = [], 0, False
+    switched, t_switch, best, since = None, None, np.inf, 0
+    while not conv and n < args.max_iter and time.perf_counter() - t0 < args.budget:
+        n += 1
+        inst.MDE_q()
+        inst.MDE_qstar()
+        d = inst.density(want_junction=False)
+        fe = inst.free_energy()
+        err, conv = inst.iterate(mp)
+        r = float(max(err[:3]))
+        hist.append([n, fe, d["lnQ"], r])
+        if not np.isfinite(r):
+            break
+        if form == "fp32" and switched is None and not conv:
+            if r < 0.98 * best:
+                best, since = r, 0
+            else:
+                since += 1
+            if n > 20 and (r < args.switch_tol or (since >= args.stall and best < 1e-3)):
                 inst.set_precision(wlc.WLC_FP64)
-                switched = n
-                t_switch = time.perf_counter() - t0
-        torch.cuda.synchronize()
-        secs = time.perf_counter() - t0
-        if args.save_w:
-            np.save(args.save_w, inst.get_fields())
-        fp32_err = None
-        if prec == wlc.WLC_FP32 and switched is None:
-            # the FP32 form's error at its final fields: the same fields
-            # evaluated by the FP64 propagators
-            w_fin = inst.get_fields()
-            vals = {}
-            for pr in (wlc.WLC_FP32, wlc.WLC_FP64):
-                inst.set_precision(pr)
-                inst.set_fields(w_fin)
-                inst.MDE_q()
-                inst.MDE_qstar()
-                dd = inst.density(want_junction=False)
-                vals[pr] = (dd["lnQ"], inst.free_energy(), dd["phi"])
-            a32, a64 = vals[wlc.WLC_FP32], vals[wlc.WLC_FP64]
-            fp32_err = {"lnQ_abs": abs(a32[0] - a64[0]), "F_rel": abs(a32[1] - a64[1]) / abs(a64[1]),
-                        "phi_max_rel": float(np.abs(a32[2] - a64[2]).max() / np.abs(a64[2]).max())}
-        out["forms"][form] = {"converged": bool(conv), "iterations": n, "seconds": secs, "F": hist[-1][1],
-                              "fp32_error_vs_fp64": fp32_err,
-                              "lnQ": hist[-1][2], "residual": max(hist[-1][3:6]), "incompressibility": hist[-1][6],
-                              "switched_at": switched, "switch_seconds": t_switch,
-                              "s_per_iteration": secs / max(1, n)}
-        if args.history:
-            out["forms"][form]["history"] = hist
-        inst.close()
-        print(json.dumps({"form": form, **{k: v for k, v in out["forms"][form].items() if k != "history"}}),
-              flush=True)
-    f = out["forms"]
-    if "fp64" in f:
-        for k, v in f.items():
-            if k != "fp64":
-                v["F_rel_err_vs_fp64"] = abs(v["F"] - f["fp64"]["F"]) / abs(f["fp64"]["F"])
-                v["speedup_vs_fp64"] = f["fp64"]["seconds"] / v["seconds"]
+                inst.reset_mixing()
+                mp.num_simple, mp.min_iter = 1, 2
+                switched, t_switch = n, time.perf_counter() - t0
+    torch.cuda.synchronize()
+    secs = time.perf_counter() - t0
+    w_fin = inst.get_fields()
+    inst.close()
+    res = {"converged": bool(conv), "iterations": n, "seconds": secs, "F": hist[-1][1], "lnQ": hist[-1][2],
+           "residual": hist[-1][3], "s_per_iteration": secs / max(1, n), "switched_at": switched,
+           "switch_seconds": t_switch, "residual_every_10": [h[3] for h in hist[::10]]}
+    if args.history:
+        res["history"] = hist
+    return res, w_fin
+
+
+def run_converge(args):
+    """Time to converged F at the 64^3, L=10, Ns=200 workload (residual <=
+    --tol in every block), through the public API:
+      fp64_cold  plain FP64 from the seeded random fields N(0, 0.5^2)
+                 (capped at --budget seconds);
+      fp64_warm  plain FP64 from the learned warm start;
+      fp32_warm  FP32 propagators (FP64 Q, F, densities, residuals and
+                 Anderson least squares) from the learned warm start, FP64
+                 for the last iterations (FP32's residual floor is above 1e-6).
+    The warm start is the network (--ws-load) evaluated at this instance's
+    parameters on its 32^3 grid and Fourier-resampled to 64^3; one run per
+    noise seed (--seeds)."""
+    import wlc
+    from wlc import warmstart as ws
+    wl = workload("fp64")
+    nr = wl["n"] ** 3
+    w_cold = np.random.default_rng(2024).normal(0.0, wl["w_sigma"], size=(3, nr))
+    net = None
+    forms = args.forms.split(",")
+    if any(f.endswith("_warm") for f in forms):
+        if not args.ws_load:
+            raise SystemExit("warm forms need --ws-load (parameters saved by --workload warmstart --ws-save)")
+        net = wlc.WarmStartNet(ws.GRID, 32, seed=1)
+        net.set_params(np.load(args.ws_load))
+    out = {"metric": "time-to-converged F (64^3, L=10, Ns=200, ABC; residual <= %g)" % args.tol,
+           "config": {"workload": WORKLOAD_SINGLE, "tol": args.tol, "switch_tol": args.switch_tol,
+                      "stall": args.stall, "budget_s": args.budget,
+                      "mixing": {"anderson_depth": args.depth, "num_simple": 20, "lambda_simple": 0.1,
+                                 "lambda_anderson": args.lambda_a}},
+           "runs": []}
+    cold = None
+    if "fp64_cold" in forms:
+        cold, _ = converge_form(wl, w_cold, "fp64", args)
+        out["fp64_cold"] = cold
+        print(json.dumps({"form": "fp64_cold", **{k: v for k, v in cold.items() if k != "history"}}), flush=True)
+    for seed in [int(v) for v in args.seeds.split(",")]:
+        run = {"seed": seed}
+        w_warm = None
+        if net is not None:
+            tp = time.perf_counter()
+            w_warm = ws.predict(net, [c2_draw(seed)], grid_out=wl["n"])[0]
+            run["predict_seconds"] = time.perf_counter() - tp
+        for f in forms:
+            if f == "fp64_cold":
+                continue
+            r, _ = converge_form(wl, w_warm, "fp32" if f == "fp32_warm" else "fp64", args)
+            if f == "fp32_warm":
+                r["seconds"] += run.get("predict_seconds", 0.0)  # the prediction is part of this form's time
+            run[f] = r
+            print(json.dumps({"form": f, "seed": seed, **{k: v for k, v in r.items() if k != "history"}}),
+                  flush=True)
+        if "fp32_warm" in run and "fp64_warm" in run:
+            a, b = run["fp32_warm"], run["fp64_warm"]
+            run["F_rel_diff_fp32_warm_vs_fp64_warm"] = abs(a["F"] - b["F"]) / abs(b["F"])
+            run["speedup_vs_fp64_warm"] = b["seconds"] / a["seconds"]
+        if "fp32_warm" in run and cold is not None:
+            run["speedup_vs_fp64_cold"] = cold["seconds"] / run["fp32_warm"]["seconds"]
+            run["speedup_vs_fp64_cold_is_lower_bound"] = not cold["converged"]
+        out["runs"].append(run)
+    if net is not None:
+        net.close()
+    if out["runs"] and "fp32_warm" in out["runs"][0]:
+        med = statistics.median([r["fp32_warm"]["seconds"] for r in out["runs"]])
+        out["value"] = med
+        out["unit"] = "s (median over seeds, fp32_warm)"
+        out["e2e"] = {"value": med, "unit": "s", "h2d_bytes_per_step": 3 * nr * 8,
+                      "d2h_bytes_per_step": 3 * nr * 8 + 24}
     print(json.dumps(out))
 
 
@@ -712,161 +746,73 @@ def run_large(args):
     inst.close()
 
 
-WS_G, WS_NMAX, WS_L = 32, 100, 6
-
-
-def ws_draws(count, seed):
-    """Instance parameters of the warm-start data set (the batched sweep's
-    ranges): fA, fC ~ U(0.2, 0.4), chiN ~ U(12, 24), L/lp ~ U(0.5, 3.0),
-    box 4.0 Rg; and the 16^3 noise seed of each instance."""
-    rng = np.random.default_rng(seed)
-    out = []
-    for i in range(count):
-        out.append(dict(fa=rng.uniform(0.2, 0.4), fc=rng.uniform(0.2, 0.4), chi=rng.uniform(12.0, 24.0),
-                        x=rng.uniform(0.5, 3.0), noise_seed=int(rng.integers(1 << 31))))
-    return out
-
-
-def ws_noise(seed):
-    """16^3 N(0, 1) noise, nearest-upsampled to the 32^3 grid."""
-    xi = np.random.default_rng(seed).normal(size=(16, 16, 16))  # [z][y][x]
-    return xi.repeat(2, 0).repeat(2, 1).repeat(2, 2).reshape(-1)
-
-
-def ws_spec(d):
-    import wlc
-    box = 4.0 * wlc.wlc_radius_of_gyration(d["x"])
-    return dict(n=WS_G, lmax=WS_L, nmax=WS_NMAX, ns=wlc.even_block_lengths((d["fa"], 1 - d["fa"] - d["fc"], d["fc"]),
-                                                                          WS_NMAX),
-                dx=box / WS_G, loa=d["x"] * 0.5, kappa=(0.5, 0.5, 0.5), chi=(d["chi"],) * 3)
-
-
-def ws_input(d):
-    """network input (6, G^3): the noise field and the five parameters
-    (scaled to about [-1, 1]) as constant fields"""
-    import wlc
-    box = 4.0 * wlc.wlc_radius_of_gyration(d["x"])
-    par = [(d["fa"] - 0.3) / 0.1, (d["fc"] - 0.3) / 0.1, (d["chi"] - 18.0) / 6.0, (d["x"] - 1.75) / 1.25,
-           box - 1.0]
-    P = WS_G ** 3
-    return np.concatenate([ws_noise(d["noise_seed"])[None, :], np.repeat(np.array(par)[:, None], P, axis=1)])
-
-
-def ws_cold(d):
-    xi = ws_noise(d["noise_seed"])
-    return 0.3 * np.stack([xi, -xi, np.zeros_like(xi)])
-
-
-def ws_solve(draws, w0s, iters, tol=0.0):
-    """SCFT of all draws together (one batch, FP32 propagators, field update
-    on the device) from the given fields; returns final fields and the
-    per-iteration max block residual of every instance."""
-    import wlc
-    b = wlc.Batch([ws_spec(d) for d in draws])
-    for inst, w0 in zip(b.instances, w0s):
-        inst.set_fields(w0)
-    b.autotune()
-    mp = wlc.mix_params(anderson_depth=5)
-    res = np.full((len(draws), iters), np.nan)
-    fe = np.full((len(draws), iters), np.nan)
-    bad = np.zeros(len(draws), dtype=bool)  # iteration diverged (non-finite density): frozen
-    for it in range(iters):
-        b.propagate()
-        for j, inst in enumerate(b.instances):
-            if bad[j]:
-                continue
-            try:
-                inst.density(want_junction=False)
-                fe[j, it] = inst.free_energy()
-                err, conv = inst.iterate(mp)
-                res[j, it] = max(err[:3])
-            except wlc.WlcError:
-                bad[j] = True
-        if tol > 0 and (res[~bad, it] < tol).all():
-            res, fe = res[:, :it + 1], fe[:, :it + 1]
-            break
-    ws = [None if bad[j] else inst.get_fields() for j, inst in enumerate(b.instances)]
-    b.close()
-    return ws, res, fe
-
-
 def run_warmstart(args):
-    """Learned warm start: solver-generated training fields (32^3, l <= 6,
-    Ns = 100, the batched sweep's parameter ranges, fields after
-    --ws-iters iterations from the cold start), network training on the
-    device, then warm vs cold starts on held-out draws."""
+    """Learned warm start at 32^3, l <= 6, Ns = 100 over the batched
+    sweep's parameter ranges (box 3.5-5.5 Rg): solver-generated converged
+    fields (bootstrapped, wlc.warmstart.generate_dataset), network training
+    on the device, then cold against warm starts on held-out draws (same
+    batches and mixing), and the final free energy of converged warm-started
+    draws re-evaluated with FP64 propagators."""
     import torch
     import wlc
+    from wlc import warmstart as ws
     t0 = time.perf_counter()
-    ntr, nte = args.ws_train, args.ws_test
-    draws = ws_draws(ntr + nte, 11)
-    train, test = draws[:ntr], draws[ntr:]
-    # training data: the solver's fields after ws_iters iterations
-    targets, kept = [], []
-    chunk = 64
-    for c0 in range(0, ntr, chunk):
-        part = train[c0:c0 + chunk]
-        ws, _, _ = ws_solve(part, [ws_cold(d) for d in part], args.ws_iters)
-        for d, w in zip(part, ws):
-            if w is None or not np.isfinite(w).all():
-                continue
-            targets.append((w - w.mean(axis=1, keepdims=True)) / d["chi"])
-            kept.append(d)
-    n_diverged_train = ntr - len(kept)
-    train = kept
-    t_data = time.perf_counter() - t0
-    X = np.stack([ws_input(d) for d in train]).astype(np.float32)
-    T = np.stack(targets).astype(np.float32)
-    net = wlc.WarmStartNet(WS_G, 32, seed=1)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    hist = net.train(X, T, batch=8, epochs=args.ws_epochs, lr=args.ws_lr)
-    torch.cuda.synchronize()
-    t_train = time.perf_counter() - t1
-    # held-out draws: cold start vs the network's fields
-    Xte = np.stack([ws_input(d) for d in test]).astype(np.float32)
-    t2 = time.perf_counter()
-    warm0 = [net.forward(x).astype(np.float64) * d["chi"] for x, d in zip(Xte, test)]
-    t_pred = time.perf_counter() - t2
-    wc, res_c, fe_c = ws_solve(test, [ws_cold(d) for d in test], args.ws_eval_iters)
-    # held-out error of the network against the solver's fields after as many iterations
-    ok = [j for j, w in enumerate(wc) if w is not None and np.isfinite(w).all()]
-    tt = {j: (wc[j] - wc[j].mean(axis=1, keepdims=True)) / test[j]["chi"] for j in ok}
-    test_mse = float(np.mean([np.mean((net.forward(Xte[j]) - tt[j]) ** 2) for j in ok]))
-    test_var = float(np.mean([np.mean(tt[j] ** 2) for j in ok]))
-    _, res_w, fe_w = ws_solve(test, warm0, args.ws_eval_iters)
-    both_ok = [j for j in range(len(test)) if np.isfinite(res_c[j, -1]) and np.isfinite(res_w[j, -1])]
-    n_div_cold = int(sum(not np.isfinite(res_c[j, -1]) for j in range(len(test))))
-    n_div_warm = int(sum(not np.isfinite(res_w[j, -1]) for j in range(len(test))))
-    res_c, res_w, fe_c, fe_w = res_c[both_ok], res_w[both_ok], fe_c[both_ok], fe_w[both_ok]
+    out = {"metric": "learned warm start: iterations to a residual, warm vs cold (32^3, L=6, Ns=100)"}
+    if args.ws_load:
+        net = wlc.WarmStartNet(ws.GRID, 32, seed=1)
+        net.set_params(np.load(args.ws_load))
+        out["network"] = {"loaded": os.path.basename(args.ws_load)}
+    else:
+        draws, targets, recs = ws.generate_dataset(args.ws_target, seed=1000, tol=args.ws_tol,
+                                                   budget_s=args.ws_budget, log=lambda m: print(m, flush=True))
+        t_data = time.perf_counter() - t0
+        cold = [r for r in recs if r["start"] == "cold"]
+        warm = [r for r in recs if r["start"] == "warm"]
 
-    def first_below(res, thr):
-        out = []
-        for r in res:
-            k = np.nonzero(r < thr)[0]
-            out.append(int(k[0]) + 1 if k.size else None)
-        return out
-
-    summary = {}
-    for thr in (1e-1, 3e-2, 1e-2, 3e-3, 1e-3):
-        c, w = first_below(res_c, thr), first_below(res_w, thr)
-        both = [(a, b) for a, b in zip(c, w) if a is not None and b is not None]
-        summary["%g" % thr] = {"cold_reached": sum(a is not None for a in c), "warm_reached": sum(b is not None for b in w),
-                               "median_cold_iters": float(np.median([a for a, _ in both])) if both else None,
-                               "median_warm_iters": float(np.median([b for _, b in both])) if both else None}
-    line = {"metric": "learned warm start: iterations to a residual, warm vs cold (32^3, L=6, Ns=100)",
-            "train_instances": len(train), "train_diverged": n_diverged_train, "test_instances": nte,
-            "test_diverged": {"cold": n_div_cold, "warm": n_div_warm}, "data_iterations": args.ws_iters,
-            "params": int(net.np), "epochs": args.ws_epochs, "lr": args.ws_lr,
-            "train_loss_first_last": [float(hist[0]), float(hist[-1])], "train_loss": [float(v) for v in hist],
-            "test_mse": test_mse, "test_target_mean_square": test_var,
-            "seconds": {"data": t_data, "train": t_train, "predict_all": t_pred},
-            "eval_iterations": args.ws_eval_iters, "thresholds": summary,
-            "median_final_residual": {"cold": float(np.median(res_c[:, -1])), "warm": float(np.median(res_w[:, -1]))},
-            "median_residual_at_50": {"cold": float(np.median(res_c[:, min(49, res_c.shape[1] - 1)])),
-                                      "warm": float(np.median(res_w[:, min(49, res_w.shape[1] - 1)]))},
-            "median_abs_F_diff_final": float(np.median(np.abs(fe_c[:, -1] - fe_w[:, -1])))}
-    print(json.dumps(line))
+        def med(rs):
+            v = [r["iterations"] for r in rs if r["iterations"] is not None]
+            return float(np.median(v)) if v else None
+        out["dataset"] = {"converged_fields": len(draws), "tolerance": args.ws_tol, "seconds": t_data,
+                          "cold_draws": len(cold), "cold_converged": sum(r["iterations"] is not None for r in cold),
+                          "warm_draws": len(warm), "warm_converged": sum(r["iterations"] is not None for r in warm),
+                          "median_iterations_cold": med(cold), "median_iterations_warm": med(warm)}
+        print(json.dumps(out["dataset"]), flush=True)
+        t1 = time.perf_counter()
+        net, hist = ws.train(draws, targets, epochs=args.ws_epochs, lr=args.ws_lr)
+        torch.cuda.synchronize()
+        out["network"] = {"params": int(net.np), "train_samples": len(draws), "epochs": args.ws_epochs,
+                          "lr": args.ws_lr, "seconds": time.perf_counter() - t1,
+                          "loss_first_last": [float(hist[0]), float(hist[-1])]}
+        if args.ws_save:
+            np.save(args.ws_save, net.params())
+        print(json.dumps(out["network"]), flush=True)
+    test = ws.draw_params(args.ws_test, 777)
+    res, summary = ws.evaluate(net, test, tol=args.ws_eval_tol, max_iter=args.ws_eval_iters)
+    out["evaluation"] = {"held_out_draws": len(test), "max_iterations": args.ws_eval_iters, "thresholds": summary,
+                         "seconds": {k: res[k]["seconds"] for k in ("cold", "warm")},
+                         "diverged": {k: sum(r["diverged"] for r in res[k]["results"]) for k in ("cold", "warm")},
+                         "median_final_residual": {k: float(np.nanmedian([r["residual"] for r in res[k]["results"]]))
+                                                   for k in ("cold", "warm")}}
+    # converged warm-started draws: F of the FP32 run against FP64 propagators at the same fields
+    checks = []
+    for d, r in zip(test, res["warm"]["results"]):
+        if r["iterations"] is None or len(checks) >= args.ws_f_checks:
+            continue
+        vals = {}
+        for prec in (wlc.WLC_FP32, wlc.WLC_FP64):
+            inst = wlc.Instance(precision=prec, store_qstar=1, **ws.instance_spec(d))
+            inst.set_fields(r["fields"])
+            inst.MDE_q()
+            inst.MDE_qstar()
+            dd = inst.density(want_junction=False)
+            vals[prec] = (inst.free_energy(), dd["lnQ"])
+            inst.close()
+        f32, f64 = vals[wlc.WLC_FP32][0], vals[wlc.WLC_FP64][0]
+        checks.append({"F_fp32": f32, "F_fp64": f64, "rel": abs(f32 - f64) / abs(f64),
+                       "lnQ_fp64": vals[wlc.WLC_FP64][1], "residual": r["residual"]})
+    out["evaluation"]["F_fp32_vs_fp64_at_converged_fields"] = checks
+    out["seconds_total"] = time.perf_counter() - t0
+    print(json.dumps(out))
     net.close()
 
 
@@ -881,30 +827,33 @@ def main():
     ap.add_argument("--profile", action="store_true", help="small-footprint case for ncu captures")
     ap.add_argument("--converge", action="store_true", help="time-to-converged F instead of steps/s")
     ap.add_argument("--workload", default="single", choices=["single", "batch", "large", "warmstart"])
-    ap.add_argument("--ws-train", type=int, default=128)
-    ap.add_argument("--ws-test", type=int, default=32)
-    ap.add_argument("--ws-iters", type=int, default=250)
-    ap.add_argument("--ws-epochs", type=int, default=40)
-    ap.add_argument("--ws-eval-iters", type=int, default=250)
-    ap.add_argument("--ws-lr", type=float, default=1e-4)
+    ap.add_argument("--ws-target", type=int, default=2000, help="warm start: converged training fields wanted")
+    ap.add_argument("--ws-budget", type=float, default=1800.0, help="warm start: data generation seconds at most")
+    ap.add_argument("--ws-tol", type=float, default=1e-4, help="warm start: residual of a converged training field")
+    ap.add_argument("--ws-test", type=int, default=200, help="warm start: held-out draws")
+    ap.add_argument("--ws-epochs", type=int, default=20)
+    ap.add_argument("--ws-eval-iters", type=int, default=400)
+    ap.add_argument("--ws-eval-tol", type=float, default=2e-6)
+    ap.add_argument("--ws-lr", type=float, default=3e-4)
+    ap.add_argument("--ws-save", default="", help="warm start: save the trained parameters (.npy)")
+    ap.add_argument("--ws-load", default="", help="warm start: load parameters instead of generating and training")
+    ap.add_argument("--ws-f-checks", type=int, default=8)
     ap.add_argument("--checkpoint", type=int, default=0, help="large workload: q checkpoint interval")
     ap.add_argument("--count", type=int, default=48, help="instances of the batched workload")
     ap.add_argument("--no-autotune", action="store_true", help="default launch configuration")
     ap.add_argument("--no-fp32", action="store_true", help="fp64 run: skip the FP32 form's line entry")
     ap.add_argument("--launch-config", default="", help="profile case: a_variant,solve_threads[,xy_threads[,xy_variant]]")
-    ap.add_argument("--forms", default="fp32sched,fp64")
+    ap.add_argument("--forms", default="fp32_warm,fp64_warm,fp64_cold")
+    ap.add_argument("--seeds", default="1,2,3", help="converge: noise seeds of the warm start")
+    ap.add_argument("--stall", type=int, default=30, help="converge: FP32 iterations without progress before FP64")
+    ap.add_argument("--stored", action="store_true", help="converge: keep every slice (overlapped sweeps)")
     ap.add_argument("--tol", type=float, default=1e-6)
-    ap.add_argument("--switch-tol", type=float, default=1e-4)
+    ap.add_argument("--switch-tol", type=float, default=1e-5)
     ap.add_argument("--depth", type=int, default=5)
     ap.add_argument("--max-iter", type=int, default=2000)
     ap.add_argument("--budget", type=float, default=900.0, help="wall-time cap per form, seconds")
     ap.add_argument("--history", action="store_true")
     ap.add_argument("--lambda-a", type=float, default=0.1, help="Anderson mixing parameter")
-    ap.add_argument("--init-w", default="", help="start from fields saved with --save-w (.npy)")
-    ap.add_argument("--seed-kind", default="random", choices=["random", "lamellar"])
-    ap.add_argument("--save-w", default="", help="save the final fields (.npy)")
-    ap.add_argument("--stop-at", type=float, default=0.0, help="stop once the residual is below this")
-    ap.add_argument("--ramp", action="store_true", help="ramp lambda_A towards 1 after the simple phase")
     args = ap.parse_args()
     if args.profile:
         run_profile_case(args)

@@ -219,6 +219,10 @@ template <typename T> static int alloc_fields(wlc_ctx* c) {
     c->qb = pt;
     if ((rc = dalloc(c, &pc, sizeof(C) * (size_t)c->nk * c->M))) return rc;
     c->phat = pc;
+    if (c->st2) {  // k-space buffer of the overlapped backward sweep
+        if ((rc = dalloc(c, &pc, sizeof(C) * (size_t)c->nk * c->M))) return rc;
+        c->phat2 = pc;
+    }
     if ((rc = dalloc(c, &pt, sizeof(T) * 15 * (size_t)c->nr))) return rc;  // cf[3][3][nr] + dsw[3][nr] + ehalf[3][nr]
     c->cf = pt;
     if ((rc = dalloc(c, &pt, sizeof(T) * sl))) return rc;
@@ -277,7 +281,7 @@ template <typename T> static int use_precision(wlc_ctx* c) {
         c->have_piv = ps.have_piv;
     }
     if (c->elem < sizeof(T)) {  // widen the propagator buffers
-        for (void** b : {&c->qf, &c->qb, &c->phat, &c->cf, &c->work, &c->msterm}) {
+        for (void** b : {&c->qf, &c->qb, &c->phat, &c->phat2, &c->cf, &c->work, &c->msterm}) {
             if (*b) {
                 for (size_t i = 0; i < c->allocs.size(); ++i)
                     if (c->allocs[i] == *b) {
@@ -296,6 +300,7 @@ template <typename T> static int use_precision(wlc_ctx* c) {
         CK(cudaGetLastError());
     }
     c->have_fwd = c->have_bwd = c->have_density = false;
+    CK(mark_inputs(c));
     return WLC_OK;
 }
 
@@ -337,6 +342,11 @@ int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
         c->own_stream = false;
     } else {
         CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+        if (p->store_qstar == 1 && std::fabs(p->nmu) < 1.0e-5) {  // overlapped sweeps (overlap_sweeps)
+            CK(cudaStreamCreateWithFlags(&c->st2, cudaStreamNonBlocking));
+            CK(cudaEventCreateWithFlags(&c->ev_inputs, cudaEventDisableTiming));
+            CK(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+        }
     }
     apply_box(c);
     // Theta and J lists
@@ -410,6 +420,7 @@ int create_impl(const wlc_params* p, cudaStream_t ext, wlc_ctx** out) {
     if ((rc = dalloc(c, &c->stage, sizeof(double) * (size_t)c->M * nr))) return rc;
     if ((rc = dalloc(c, &c->flag, sizeof(int)))) return rc;
     CK(cudaMemsetAsync(c->mop, 0, sizeof(double) * 9 * nr, c->st));
+    CK(mark_inputs(c));
     CK(cudaStreamSynchronize(c->st));
     c->err.clear();
     return WLC_OK;
@@ -426,8 +437,12 @@ extern "C" int wlc_destroy(wlc_ctx* c) {
 int destroy_impl(wlc_ctx* c) {
     if (!c) return WLC_OK;
     if (c->st) cudaStreamSynchronize(c->st);
+    if (c->st2) cudaStreamSynchronize(c->st2);
     for (void* p : c->allocs) cudaFree(p);
     for (auto e : c->ev) cudaEventDestroy(e);
+    if (c->ev_inputs) cudaEventDestroy(c->ev_inputs);
+    if (c->ev_join) cudaEventDestroy(c->ev_join);
+    if (c->st2) cudaStreamDestroy(c->st2);
     if (c->st && c->own_stream) cudaStreamDestroy(c->st);
     delete c;
     return WLC_OK;
@@ -447,6 +462,7 @@ extern "C" int wlc_set_box(wlc_ctx* c, double dx, double dy, double dz) {
     ps.have_piv = c->have_piv;
     ps.piv_gen = c->box_gen;
     c->have_fwd = c->have_bwd = c->have_density = false;
+    CK(mark_inputs(c));
     return WLC_OK;
 }
 
@@ -481,6 +497,7 @@ extern "C" int wlc_set_fields(wlc_ctx* c, const double* w, const double* m_op) {
     CK(cudaGetLastError());
     c->have_fields = true;
     c->have_fwd = c->have_bwd = c->have_density = false;
+    CK(mark_inputs(c));
     return WLC_OK;
 }
 
@@ -609,8 +626,24 @@ extern "C" int wlc_propagate(wlc_ctx* c, int32_t dir) {
     if (!c->have_fields) return set_err(c, WLC_E_STATE, "wlc_set_fields must be called before wlc_propagate");
     if (dir < 0 && c->stream && !c->have_fwd)
         return set_err(c, WLC_E_STATE, "with streamed densities (store_qstar 0/2) the forward sweep must come first");
-    int rc = c->fp32 ? sweep<float>(c, dir) : sweep<double>(c, dir);
-    if (rc) return rc;
+    int rc;
+    if (dir < 0 && overlap_sweeps(c)) {
+        // q* does not read q: run the backward sweep on the second stream
+        // with its own k-space buffer, after the inputs and overlapping the
+        // forward sweep; the context stream waits for it before anything else
+        CK(cudaStreamWaitEvent(c->st2, c->ev_inputs, 0));
+        std::swap(c->st, c->st2);
+        std::swap(c->phat, c->phat2);
+        rc = c->fp32 ? sweep<float>(c, dir) : sweep<double>(c, dir);
+        std::swap(c->st, c->st2);
+        std::swap(c->phat, c->phat2);
+        if (rc) return rc;
+        CK(cudaEventRecord(c->ev_join, c->st2));
+        CK(cudaStreamWaitEvent(c->st, c->ev_join, 0));
+    } else {
+        rc = c->fp32 ? sweep<float>(c, dir) : sweep<double>(c, dir);
+        if (rc) return rc;
+    }
     if (dir > 0)
         c->have_fwd = true;
     else
@@ -768,7 +801,10 @@ extern "C" int wlc_set_q(wlc_ctx* c, int32_t dir, int32_t s, const double* in) {
         return set_err(c, WLC_E_PARAM, "wlc_set_q: bad dir / s / in");
     if ((dir > 0 && c->K) || (dir < 0 && c->stream))
         return set_err(c, WLC_E_STATE, "that propagator is not stored (store_qstar / q_checkpoint)");
-    return c->fp32 ? set_q<float>(c, dir, s, in) : set_q<double>(c, dir, s, in);
+    const int rc = c->fp32 ? set_q<float>(c, dir, s, in) : set_q<double>(c, dir, s, in);
+    if (rc) return rc;
+    CK(mark_inputs(c));
+    return WLC_OK;
 }
 
 template <typename T> static int init_pr_impl(wlc_ctx* c, int dir, int s, double* pr) {
@@ -993,6 +1029,7 @@ extern "C" int wlc_iterate(wlc_ctx* c, const wlc_mix_params* mp, double* err, in
         launch_make_cf<double>(c->w, (double*)c->cf, c->ds, third, c->nr, c->st);
     c->launches++;
     CK(cudaGetLastError());
+    CK(mark_inputs(c));
     // convergence test (SCFT_iterate.f90:1124-1160) and the minimum iteration
     // count of the driver loop (SCFT_control.f90:270-272)
     const bool strict = err[0] < mp->tol && err[1] < mp->tol && err[2] < mp->tol &&

@@ -29,6 +29,13 @@ struct wlc_ctx {
     int nkeys = 0, npiv = 0;
     bool have_piv = false;
     cudaStream_t st = nullptr;
+    // overlapped sweeps (stored mode, own stream): the backward sweep runs on
+    // st2 with its own k-space buffer phat2, after ev_inputs (recorded on st
+    // by every call that changes what the sweep reads) and before ev_join
+    // (which st waits on), so it overlaps the forward sweep on st
+    cudaStream_t st2 = nullptr;
+    cudaEvent_t ev_inputs = nullptr, ev_join = nullptr;
+    void* phat2 = nullptr;
     std::string err;
     BasisTables tab;
     std::vector<void*> allocs;
@@ -228,6 +235,17 @@ inline StepLaunch<T> make_launch(wlc_ctx* c, StepKind k, const T* h1, const T* h
     }
     return L;
 }
+
+// the backward sweep may run on its own stream, overlapping the forward
+// sweep: q* does not depend on q when every slice is stored (the densities
+// come after both sweeps); not with streamed densities, the Maier-Saupe term
+// (one Theta buffer), timing (per-pass events) or a stream shared with a batch
+inline bool overlap_sweeps(const wlc_ctx* c) {
+    return c->st2 && c->phat2 && c->p.store_qstar == 1 && !ms_on(c) && !c->timing && !c->batch_owned;
+}
+// the inputs of a backward sweep (fields, coefficient planes, tables, box,
+// stored slices) are final up to here on the context stream
+inline cudaError_t mark_inputs(wlc_ctx* c) { return c->ev_inputs ? cudaEventRecord(c->ev_inputs, c->st) : cudaSuccess; }
 
 // slice addressing of the storage modes
 template <typename T> inline T* qf_ring(wlc_ctx* c, int s) {
