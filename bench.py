@@ -630,6 +630,15 @@ def run_batch(args):
     launches = b.launch_count - l0
     steps = 2 * 128 * len(specs) * args.steps
     value = steps / (ms / 1000.0)
+    # the same batched launches issued directly instead of replayed as a graph
+    b.use_graph(False)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        b.propagate()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms_direct = ev0.elapsed_time(ev1)
+    b.use_graph(True)
     # the same instances swept one by one (no batching, no graph)
     ev0.record(stream)
     for _ in range(args.steps):
@@ -670,6 +679,10 @@ def run_batch(args):
                        "autotuned": cfg},
             "unbatched": {"value": steps / (ms_seq / 1000.0), "unit": "steps/s",
                           "note": "same instances swept one after another, one launch per pass per instance"},
+            "graph": {"ms_per_propagate": ms / args.steps, "direct_ms_per_propagate": ms_direct / args.steps,
+                      "launches_per_propagate": launches / args.steps,
+                      "note": "one propagate = forward + backward sweep of every instance; direct = the same "
+                              "batched launches issued one by one instead of replayed as a CUDA graph"},
             "e2e": {"value": e2e, "unit": "steps/s", "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps},
             "gpu_launches": int(launches), "clocks": clocks}
