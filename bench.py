@@ -489,6 +489,8 @@ def converge_form(wl, w0, form, args):
         hist.append([n, fe, d["lnQ"], r])
         if not np.isfinite(r):
             break
+        if args.lambda_late > 0 and n > 20 and r < args.late_below:
+            mp.lambda_anderson = args.lambda_late  # larger Anderson weight close to the solution
         if form == "fp32" and switched is None and not conv:
             if r < 0.98 * best:
                 best, since = r, 0
@@ -539,7 +541,8 @@ def run_converge(args):
            "config": {"workload": WORKLOAD_SINGLE, "tol": args.tol, "switch_tol": args.switch_tol,
                       "stall": args.stall, "budget_s": args.budget,
                       "mixing": {"anderson_depth": args.depth, "num_simple": 20, "lambda_simple": 0.1,
-                                 "lambda_anderson": args.lambda_a}},
+                                 "lambda_anderson": args.lambda_a, "lambda_late": args.lambda_late,
+                                 "late_below": args.late_below}},
            "runs": []}
     cold = None
     if "fp64_cold" in forms:
@@ -860,6 +863,9 @@ def main():
     ap.add_argument("--seeds", default="1,2,3", help="converge: noise seeds of the warm start")
     ap.add_argument("--stall", type=int, default=30, help="converge: FP32 iterations without progress before FP64")
     ap.add_argument("--stored", action="store_true", help="converge: keep every slice (overlapped sweeps)")
+    ap.add_argument("--lambda-late", type=float, default=0.0, help="converge: Anderson weight once the residual "
+                    "is below --late-below (0: keep --lambda-a)")
+    ap.add_argument("--late-below", type=float, default=1e-3)
     ap.add_argument("--tol", type=float, default=1e-6)
     ap.add_argument("--switch-tol", type=float, default=1e-5)
     ap.add_argument("--depth", type=int, default=5)
