@@ -301,23 +301,11 @@ __device__ __forceinline__ void stage_tile(const T* __restrict__ a, const T* __r
 }
 
 // q^T J_t q* at one point from staged vectors (stride TILE) and staged lists
-// (four independent partial sums: the list entries and coefficient loads of
-// four terms are in flight together instead of one serial chain; the
-// stored-mode and streamed kernels share this order)
 template <typename T> __device__ __forceinline__ double jt_form(const SliceSmem<T>& m, int t, int k) {
     constexpr int TILE = PointTile<T>::value;
-    auto term = [&](int e) -> T { return m.jval[e] * m.sa[m.jrow[e] * TILE + k] * m.sc[m.jcol[e] * TILE + k]; };
-    T v0 = (T)0, v1 = (T)0, v2 = (T)0, v3 = (T)0;
-    const int e1 = m.jptr[t + 1];
-    int e = m.jptr[t];
-    for (; e + 4 <= e1; e += 4) {
-        v0 += term(e);
-        v1 += term(e + 1);
-        v2 += term(e + 2);
-        v3 += term(e + 3);
-    }
-    for (; e < e1; ++e) v0 += term(e);
-    return (double)((v0 + v1) + (v2 + v3));
+    T v = (T)0;
+    for (int e = m.jptr[t]; e < m.jptr[t + 1]; ++e) v += m.jval[e] * m.sa[m.jrow[e] * TILE + k] * m.sc[m.jcol[e] * TILE + k];
+    return (double)v;
 }
 
 // orientation tensor per block (SCFT_Density_FE.f90:161-220):
