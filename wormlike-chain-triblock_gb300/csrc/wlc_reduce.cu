@@ -111,7 +111,15 @@ template <typename T> __device__ __forceinline__ void vstore(T* p, const T* v) {
     *reinterpret_cast<typename VecOf<T>::t*>(p) = x;
 }
 
-// shared-memory layout of ms_term: hc[M][TILE] (16-byte aligned rows) | val[5n] | rowptr[M+1] | col[n]
+// the first four basis-tensor values of one Theta-list entry, one 16-byte
+// (FP32) or two 16-byte (FP64) shared loads
+template <typename T> struct alignas(16) Val4 {
+    T v[4];
+};
+
+// shared-memory layout of ms_term: hc[M][TILE] (16-byte aligned rows) |
+// val4[n] | val5[n] | rowptr[M+1] | col[n] (the same bytes as five values
+// and a column per entry, in three loads per entry instead of six)
 template <typename T> __host__ __device__ inline size_t ms_smem_bytes(int n, int M) {
     return sizeof(T) * ((size_t)5 * n + (size_t)M * PointTile<T>::value) + sizeof(int) * (size_t)(M + 1) +
            sizeof(int16_t) * (size_t)n;
@@ -128,10 +136,16 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
     constexpr int TILE = PointTile<T>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* hc = reinterpret_cast<T*>(smem_raw);  // [M][TILE]: BDF history combination of the tile's points
-    T* sval = hc + (size_t)M * TILE;
-    int* srp = reinterpret_cast<int*>(sval + (size_t)5 * tl.n);
+    Val4<T>* sv4 = reinterpret_cast<Val4<T>*>(hc + (size_t)M * TILE);  // M TILE sizeof(T) bytes in: 16-aligned
+    T* sv5 = reinterpret_cast<T*>(sv4 + tl.n);
+    int* srp = reinterpret_cast<int*>(sv5 + tl.n);
     int16_t* scol = reinterpret_cast<int16_t*>(srp + M + 1);
-    for (int e = threadIdx.x; e < 5 * tl.n; e += blockDim.x) sval[e] = (T)tl.val[e];
+    for (int e = threadIdx.x; e < tl.n; e += blockDim.x) {
+        Val4<T> x;
+        for (int c = 0; c < 4; ++c) x.v[c] = (T)tl.val[5 * e + c];
+        sv4[e] = x;
+        sv5[e] = (T)tl.val[5 * e + 4];
+    }
     for (int e = threadIdx.x; e <= M; e += blockDim.x) srp[e] = tl.rowptr[e];
     for (int e = threadIdx.x; e < tl.n; e += blockDim.x) scol[e] = tl.col[e];
     const int k = threadIdx.x % TILE, g = threadIdx.x / TILE;
@@ -175,8 +189,8 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
         // entries in groups of four with independent partial sums (the list
         // loads and the coefficient gathers of four entries overlap)
         auto term = [&](int e) -> T {
-            const T* v5 = sval + 5 * e;
-            const T th = coef[0] * v5[0] + coef[1] * v5[1] + coef[2] * v5[2] + coef[3] * v5[3] + coef[4] * v5[4];
+            const Val4<T> x = sv4[e];
+            const T th = coef[0] * x.v[0] + coef[1] * x.v[1] + coef[2] * x.v[2] + coef[3] * x.v[3] + coef[4] * sv5[e];
             return fabs(th) < th_min ? (T)0 : th * hv[scol[e] * TILE];
         };
         for (int i = g; i < M; i += kMsGroups) {
@@ -242,21 +256,26 @@ __global__ void density_accum(const T* __restrict__ qf, const T* __restrict__ qb
     }
 }
 
+// one J-list entry packed for a single broadcast load per entry (8 bytes
+// in FP32, 16 in FP64) instead of three loads from separate arrays
+template <typename T> struct alignas(sizeof(T) == 8 ? 16 : 8) JEnt {
+    T val;
+    int16_t row, col;
+};
+
 // shared-memory layout of the tiled density / tensor kernels:
-// sa[M][TILE] | sc[M][TILE] | jval[nj] | jptr[6] | jrow[nj] | jcol[nj]
+// sa[M][TILE] | sc[M][TILE] | jent[nj] | jptr[6]
 template <typename T> __host__ __device__ inline size_t slice_smem_bytes(int M, int nj, bool want_s) {
     size_t b = 2 * sizeof(T) * (size_t)M * PointTile<T>::value;
-    if (want_s) b += sizeof(T) * (size_t)nj + sizeof(int) * 6 + 2 * sizeof(int16_t) * (size_t)nj;
+    if (want_s) b += sizeof(JEnt<T>) * (size_t)nj + sizeof(int) * 6;
     return b;
 }
 
 template <typename T> struct SliceSmem {
     T* sa;
     T* sc;
-    T* jval;
+    JEnt<T>* jent;
     int* jptr;
-    int16_t* jrow;
-    int16_t* jcol;
 };
 
 template <typename T> __device__ __forceinline__ SliceSmem<T> slice_smem(unsigned char* raw, int M, int nj) {
@@ -264,18 +283,18 @@ template <typename T> __device__ __forceinline__ SliceSmem<T> slice_smem(unsigne
     SliceSmem<T> m;
     m.sa = reinterpret_cast<T*>(raw);
     m.sc = m.sa + (size_t)M * TILE;
-    m.jval = m.sc + (size_t)M * TILE;
-    m.jptr = reinterpret_cast<int*>(m.jval + nj);
-    m.jrow = reinterpret_cast<int16_t*>(m.jptr + 6);
-    m.jcol = m.jrow + nj;
+    m.jent = reinterpret_cast<JEnt<T>*>(m.sc + (size_t)M * TILE);  // 2 M TILE sizeof(T) bytes in: 16-aligned
+    m.jptr = reinterpret_cast<int*>(m.jent + nj);
     return m;
 }
 
 template <typename T> __device__ __forceinline__ void stage_jlists(const JLists& jl, const SliceSmem<T>& m) {
     for (int e = threadIdx.x; e < jl.n; e += blockDim.x) {
-        m.jval[e] = (T)jl.val[e];
-        m.jrow[e] = jl.row[e];
-        m.jcol[e] = jl.col[e];
+        JEnt<T> x;
+        x.val = (T)jl.val[e];
+        x.row = jl.row[e];
+        x.col = jl.col[e];
+        m.jent[e] = x;
     }
     for (int e = threadIdx.x; e < 6; e += blockDim.x) m.jptr[e] = jl.ptr[e];
 }
@@ -304,7 +323,10 @@ __device__ __forceinline__ void stage_tile(const T* __restrict__ a, const T* __r
 template <typename T> __device__ __forceinline__ double jt_form(const SliceSmem<T>& m, int t, int k) {
     constexpr int TILE = PointTile<T>::value;
     T v = (T)0;
-    for (int e = m.jptr[t]; e < m.jptr[t + 1]; ++e) v += m.jval[e] * m.sa[m.jrow[e] * TILE + k] * m.sc[m.jcol[e] * TILE + k];
+    for (int e = m.jptr[t]; e < m.jptr[t + 1]; ++e) {
+        const JEnt<T> x = m.jent[e];
+        v += x.val * m.sa[x.row * TILE + k] * m.sc[x.col * TILE + k];
+    }
     return (double)v;
 }
 
