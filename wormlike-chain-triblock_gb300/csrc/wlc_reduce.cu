@@ -111,15 +111,7 @@ template <typename T> __device__ __forceinline__ void vstore(T* p, const T* v) {
     *reinterpret_cast<typename VecOf<T>::t*>(p) = x;
 }
 
-// the first four basis-tensor values of one Theta-list entry, one 16-byte
-// (FP32) or two 16-byte (FP64) shared loads
-template <typename T> struct alignas(16) Val4 {
-    T v[4];
-};
-
-// shared-memory layout of ms_term: hc[M][TILE] (16-byte aligned rows) |
-// val4[n] | val5[n] | rowptr[M+1] | col[n] (the same bytes as five values
-// and a column per entry, in three loads per entry instead of six)
+// shared-memory layout of ms_term: hc[M][TILE] (16-byte aligned rows) | val[5n] | rowptr[M+1] | col[n]
 template <typename T> __host__ __device__ inline size_t ms_smem_bytes(int n, int M) {
     return sizeof(T) * ((size_t)5 * n + (size_t)M * PointTile<T>::value) + sizeof(int) * (size_t)(M + 1) +
            sizeof(int16_t) * (size_t)n;
@@ -136,16 +128,10 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
     constexpr int TILE = PointTile<T>::value;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     T* hc = reinterpret_cast<T*>(smem_raw);  // [M][TILE]: BDF history combination of the tile's points
-    Val4<T>* sv4 = reinterpret_cast<Val4<T>*>(hc + (size_t)M * TILE);  // M TILE sizeof(T) bytes in: 16-aligned
-    T* sv5 = reinterpret_cast<T*>(sv4 + tl.n);
-    int* srp = reinterpret_cast<int*>(sv5 + tl.n);
+    T* sval = hc + (size_t)M * TILE;
+    int* srp = reinterpret_cast<int*>(sval + (size_t)5 * tl.n);
     int16_t* scol = reinterpret_cast<int16_t*>(srp + M + 1);
-    for (int e = threadIdx.x; e < tl.n; e += blockDim.x) {
-        Val4<T> x;
-        for (int c = 0; c < 4; ++c) x.v[c] = (T)tl.val[5 * e + c];
-        sv4[e] = x;
-        sv5[e] = (T)tl.val[5 * e + 4];
-    }
+    for (int e = threadIdx.x; e < 5 * tl.n; e += blockDim.x) sval[e] = (T)tl.val[e];
     for (int e = threadIdx.x; e <= M; e += blockDim.x) srp[e] = tl.rowptr[e];
     for (int e = threadIdx.x; e < tl.n; e += blockDim.x) scol[e] = tl.col[e];
     const int k = threadIdx.x % TILE, g = threadIdx.x / TILE;
@@ -189,8 +175,8 @@ __global__ void __launch_bounds__(PointTile<T>::value * kMsGroups)
         // entries in groups of four with independent partial sums (the list
         // loads and the coefficient gathers of four entries overlap)
         auto term = [&](int e) -> T {
-            const Val4<T> x = sv4[e];
-            const T th = coef[0] * x.v[0] + coef[1] * x.v[1] + coef[2] * x.v[2] + coef[3] * x.v[3] + coef[4] * sv5[e];
+            const T* v5 = sval + 5 * e;
+            const T th = coef[0] * v5[0] + coef[1] * v5[1] + coef[2] * v5[2] + coef[3] * v5[3] + coef[4] * v5[4];
             return fabs(th) < th_min ? (T)0 : th * hv[scol[e] * TILE];
         };
         for (int i = g; i < M; i += kMsGroups) {
