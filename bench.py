@@ -712,11 +712,23 @@ def run_large(args):
     K = args.checkpoint or int(round((3 * nmax) ** 0.5))
     inst = wlc.Instance(n, L, nmax, ns, box / n, x * 0.5, (0.5, 0.5, 0.5), (20.0, 20.0, 20.0), nmu=5.0,
                         precision=wlc.WLC_FP32, store_qstar=2, q_checkpoint=K)
-    g = 2 * np.pi * np.arange(n) / n
-    X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
-    gyr = (np.sin(X) * np.cos(Y) + np.sin(Y) * np.cos(Z) + np.sin(Z) * np.cos(X)).transpose(2, 1, 0).reshape(-1)
-    rng = np.random.default_rng(77)
-    w = np.stack([gyr, -gyr, 0.5 * gyr]) + rng.normal(0.0, 0.05, size=(3, n ** 3))
+    if args.ws_load:
+        # learned warm start: the 32^3 network's fields for a 4 Rg box at these
+        # parameters (contour/persistence clipped to the training range),
+        # tiled 2 x 2 x 2 and resampled to 128^3
+        from wlc import warmstart as ws
+        net = wlc.WarmStartNet(ws.GRID, 32, seed=1)
+        net.set_params(np.load(args.ws_load))
+        w = ws.predict_large(net, dict(fa=0.3, fc=0.3, chi=20.0, x=x, box=8.0, noise_seed=77), n, 2)
+        net.close()
+        start = "learned warm start (32^3 network, 4 Rg box tiled 2x2x2, resampled)"
+    else:
+        g = 2 * np.pi * np.arange(n) / n
+        X, Y, Z = np.meshgrid(g, g, g, indexing="ij")
+        gyr = (np.sin(X) * np.cos(Y) + np.sin(Y) * np.cos(Z) + np.sin(Z) * np.cos(X)).transpose(2, 1, 0).reshape(-1)
+        rng = np.random.default_rng(77)
+        w = np.stack([gyr, -gyr, 0.5 * gyr]) + rng.normal(0.0, 0.05, size=(3, n ** 3))
+        start = "gyroid-like seeded start"
     inst.set_fields(w)
     tuned = None if args.no_autotune else inst.autotune()
     stream = torch.cuda.ExternalStream(inst.stream)
@@ -749,7 +761,7 @@ def run_large(args):
     line = {"metric": "MDE contour steps/s (128^3, L=12, Ns=400, sqrt(Ns) checkpointing, Maier-Saupe)",
             "value": mde_steps / (ms / 1000.0), "unit": "steps/s", "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (gyroid-like seeded start)",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (%s)" % start,
             "config": {"workload": "ABC triblock 128^3, box 8.0 Rg, L=12 (M=169), Ns=400 (%d/%d/%d), chiN=20, "
                                    "L/lp=4.0, muN=5; q checkpoint every %d slices, recompute per segment; one bench "
                                    "step = one SCFT iteration (%d MDE steps + %d recompute steps)" % (

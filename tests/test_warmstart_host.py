@@ -41,3 +41,15 @@ def test_draws_inputs_and_specs():
     w = np.random.default_rng(2).normal(size=(3, 8))
     t = ws.to_target(w, 15.0)
     assert np.allclose(t.mean(axis=1), 0.0) and np.allclose(ws.from_output(t, 15.0), w - w.mean(axis=1, keepdims=True))
+
+
+def test_tiling_and_range_clipping():
+    f = np.random.default_rng(5).normal(size=(3, 8 ** 3))
+    t = ws.tile_periodic(f, 2).reshape(3, 16, 16, 16)
+    g = f.reshape(3, 8, 8, 8)
+    for dz in (0, 8):
+        for dy in (0, 8):
+            for dx in (0, 8):
+                assert np.array_equal(t[:, dz:dz + 8, dy:dy + 8, dx:dx + 8], g)
+    e = ws.clamp_to_ranges(dict(fa=0.1, fc=0.3, chi=30.0, x=4.0, box=4.0, noise_seed=1))
+    assert e["fa"] == 0.2 and e["chi"] == 24.0 and e["x"] == 3.0 and e["box"] == 4.0 and e["fc"] == 0.3

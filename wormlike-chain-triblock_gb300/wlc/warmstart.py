@@ -167,6 +167,34 @@ def solve_batch(draws, w0s, max_iter, tol, mixing=None, grid=GRID, lmax=LMAX, nm
     return out
 
 
+def tile_periodic(f, reps):
+    """Periodic fields f (..., n^3, [z][y][x] flattened) repeated reps times
+    along every axis: the fields of a box reps times larger."""
+    f = np.asarray(f)
+    lead = f.shape[:-1]
+    n = round(f.shape[-1] ** (1.0 / 3.0))
+    g = np.tile(f.reshape(lead + (n, n, n)), (1,) * len(lead) + (reps, reps, reps))
+    return g.reshape(lead + ((n * reps) ** 3,))
+
+
+def clamp_to_ranges(d):
+    """The draw with every parameter clipped to the training ranges (the
+    network is not asked to extrapolate)."""
+    e = dict(d)
+    for k, (lo, hi) in RANGES.items():
+        e[k] = float(min(max(e[k], lo), hi))
+    return e
+
+
+def predict_large(net, d, grid_out, reps):
+    """Warm start of a box `reps` times the predicted one along each axis:
+    the network's fields for the box d["box"] / reps (clipped to the
+    training ranges), tiled reps^3 times and Fourier-resampled to grid_out^3."""
+    e = clamp_to_ranges(dict(d, box=d["box"] / reps))
+    w = from_output(net.forward(net_input(e, net.G)), d["chi"])
+    return fourier_resample(tile_periodic(w, reps), grid_out)
+
+
 def predict(net, draws, grid_out=None):
     """Warm-start fields of each draw from the network (grid_out^3 by
     Fourier resampling when it differs from the network's grid)."""
