@@ -45,11 +45,11 @@ def numpy_split_step(o, sigma, kappa, w, q, real4=1):
 
 
 @pytest.mark.parametrize("real4", [1, 0])
-@pytest.mark.parametrize("sigma,blk", [(1, 0), (-1, 2)])
-def test_split_step_matches_numpy_restatement(sigma, blk, real4):
+@pytest.mark.parametrize("sigma,blk,L", [(1, 0, 2), (-1, 2, 2), (1, 1, 10)])
+def test_split_step_matches_numpy_restatement(sigma, blk, L, real4):
     n = (6, 4, 8)
     kappa = (0.5, 0.7, 0.9)
-    o = oracle.Oracle(n, 2, 10, (4, 2, 4), (0.2, 0.25, 0.15), 1.3, kappa, (15, 15, 15), real4=real4, scheme=1)
+    o = oracle.Oracle(n, L, 10, (4, 2, 4), (0.2, 0.25, 0.15), 1.3, kappa, (15, 15, 15), real4=real4, scheme=1)
     rng = np.random.default_rng(5 + blk)
     w = rng.normal(0.0, 0.7, size=(3, o.nr))
     o.set_fields(w)
